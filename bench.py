@@ -1,0 +1,447 @@
+#!/usr/bin/env python3
+"""Throughput of the Melvin.py per-timestep hot path on GB300.
+
+Workload: decaying 2D turbulence, 2048 x 2048, doubly periodic, fully
+spectral (2/3 dealiasing), nu = 5e-5, dt = 2e-4, AB2 with semi-implicit
+diffusion (alpha = 0.51), second-order finite-difference Jacobian -- the
+configuration the headline metric is quoted on.  One step = velocity from
+vorticity, nonlinear term, update, i.e. one pass of the fused timestep
+(three kernels) over the resident state.
+
+Arms:
+  native     (default) the fused FP64 timestep; also the split-precision
+             (FP32 transforms / FP64 state) timestep, an end-to-end run
+             through the public API with host buffers, and the CPU
+             baseline (the NumPy oracle on the host cores, bounded sample);
+  reference  the reference algorithm's CPU implementation (the NumPy
+             oracle) on the host cores, same workload.
+
+Multi-GPU (torchrun): replicas only -- every rank advances its own
+simulation; the value is the sum over ranks with the max-over-ranks time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.join(ROOT, "melvin.py_gb300")
+if PKG_ROOT not in sys.path:
+    sys.path.insert(0, PKG_ROOT)
+
+METRIC = "Mpts·steps/s at 2048² (plain FP64 vs FP32/FP64 split); solves/s + p99 latency"
+UNIT = "Mpts·steps/s"
+WORKLOAD = {
+    "workload": "decaying 2D turbulence 2048x2048, fully spectral, AB2 semi-implicit (alpha=0.51), "
+                "FD2 Jacobian, nu=5e-5, dt=2e-4",
+    "nx": 2048, "nz": 2048, "lx": "2*pi", "lz": "2*pi", "nu": 5e-5, "dt": 2e-4,
+    "integrator_order": 2, "spatial_derivative_order": 2,
+}
+DATA = "synthetic: seeded vorticity with E(k)~k^4 exp(-(k/10)^2), uniform random phases, unit RMS velocity"
+L2_FLUSH_BYTES = 256 << 20
+
+
+# ---------------------------------------------------------------------------
+# process group helpers (replicas only: no data-path collective)
+# ---------------------------------------------------------------------------
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def dist_init(backend):
+    import torch.distributed as dist
+
+    rank, world, _ = dist_env()
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group(backend=backend, rank=rank, world_size=world)
+    return dist if world > 1 else None
+
+
+def reduce_max(value: float, dist=None, device=None) -> float:
+    """Max of a per-rank scalar over all ranks (identity for one rank)."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist=None):
+    if dist is not None:
+        dist.barrier()
+
+
+def aggregate_throughput(npts_per_rank: int, steps: int, world: int, max_seconds: float) -> float:
+    """Whole-job Mpts*steps/s: all ranks' points over the slowest rank's time."""
+    return world * npts_per_rank * steps / max_seconds / 1e6
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self._t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+
+def make_params(n, precision, device):
+    import numpy as np
+
+    import melvin
+
+    return melvin.Parameters({
+        "nx": n, "nz": n, "lx": 2 * np.pi, "lz": 2 * np.pi, "final_time": 1.0,
+        "initial_dt": WORKLOAD["dt"], "integrator_order": WORKLOAD["integrator_order"],
+        "spatial_derivative_order": WORKLOAD["spatial_derivative_order"], "integrator": "semi-implicit",
+        "precision": precision, "device": str(device),
+    })
+
+
+def make_run(n, precision, device, w0):
+    import torch
+
+    import melvin
+    from melvin import BasisFunctions as B, equations
+
+    p = make_params(n, precision, device)
+    sim = melvin.Simulation(p, torch)
+    bf = [B.COMPLEX_EXP, B.COMPLEX_EXP]
+    w = sim.make_variable("w", bf)
+    dw = sim.make_derivative("dw")
+    w.load(w0, is_physical=True)
+    step = equations.vorticity(sim, w, dw, WORKLOAD["nu"])
+    return sim, w, dw, step
+
+
+def kernel_model(n, split):
+    """Algorithmic bytes and nominal FFT flops per launch of the three
+    fused-step kernels (F = 1 advected field)."""
+    nn, nm = (n - 1) // 3, (n - 1) // 3
+    S = (2 * nn + 1) * nm  # spectral elements
+    Pk = n * nm            # x-pass intermediate elements (kept z modes only)
+    ws, wi = 16, (8 if split else 16)
+    lg = n.bit_length() - 1
+    fft = 5 * n * lg       # nominal flops of one complex length-n FFT
+    return {
+        "xinv": {"bytes": ws * S + 3 * wi * Pk, "flops": 3 * nm * fft},
+        "zstep": {"bytes": 5 * wi * Pk, "flops": (n // 2) * 5 * fft + 12 * n * n},
+        "xfwd": {"bytes": 2 * wi * Pk + 4 * ws * S, "flops": nm * fft + 30 * S},
+    }
+
+
+def timed_steps(step, steps, flush, with_kernels=True):
+    """Run `steps` fused steps; each bracketed by CUDA events on the launching
+    stream, with an L2 flush (untimed) between steps.  Returns per-step ms
+    and per-kernel ms lists."""
+    import torch
+
+    nk = step.kernel_count()
+    per_step, per_kernel = [], [[] for _ in range(nk)]
+    for _ in range(steps):
+        flush.zero_()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(nk + 1)]
+        for e in ev:
+            e.record()  # materialise the events
+        step.step_events(ev)
+        torch.cuda.synchronize()
+        per_step.append(ev[0].elapsed_time(ev[-1]))
+        for k in range(nk):
+            per_kernel[k].append(ev[k].elapsed_time(ev[k + 1]))
+    return per_step, per_kernel
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of the fused-step kernels from the committed
+    ncu summary (profiles/fused_step_traffic.json), when present."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "fused_step_traffic.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def roofline(model, kernel_ms, names, peak_gbs, peak_kind, traffic, key):
+    avg = [statistics.mean(v) for v in kernel_ms]
+    k = max(range(len(avg)), key=lambda i: avg[i])
+    name = names[k]
+    achieved = model[name]["bytes"] / (avg[k] * 1e-3) / 1e9
+    tr = traffic.get(key, {}).get(name)
+    return {
+        "kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
+        "frac": round(achieved / peak_gbs, 4), "peak_kind": peak_kind,
+        "traffic": tr, "algorithmic_bytes": model[name]["bytes"], "avg_ms": round(avg[k], 4),
+        "kernel_ms": {names[i]: round(avg[i], 4) for i in range(len(avg))},
+    }, k
+
+
+FP64_FMA_TFLOPS = 1.205  # measured on this machine's GB300 (FP64 FMA loop)
+
+
+def cpu_step_sample(w0, n, steps):
+    """The NumPy oracle (reference algorithm, single thread) on the host."""
+    import numpy as np
+
+    import oracle as O
+    from oracle import problems as P
+
+    g = O.Grid(n, n, 2 * np.pi, 2 * np.pi)
+    pr = P.Problem(g, P.vorticity_specs(WORKLOAD["nu"]), [O.to_spectral(g, w0)], WORKLOAD["dt"])
+    pr.step()  # warm
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        pr.step()
+    dt = time.perf_counter() - t0
+    return n * n * steps / dt / 1e6, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from melvin import workloads
+
+    n = args.n
+    w0 = workloads.decaying_turbulence(n, n, seed=0)
+    for _ in range(max(args.warmup - 1, 0)):
+        cpu_step_sample(w0, n, 0)
+    val, secs = cpu_step_sample(w0, n, args.steps)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(val, 4), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": dict(WORKLOAD, nx=n, nz=n),
+        "cpu_baseline": {"value": round(val, 4), "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"{args.steps} full timesteps at {n}x{n} (NumPy oracle, one thread: "
+                                   "pocketfft is single-threaded)"},
+        "e2e": {"value": round(val, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_native(args):
+    import numpy as np
+    import torch
+
+    from melvin import workloads
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    dist = dist_init("nccl")
+    n = args.n
+    w0 = workloads.decaying_turbulence(n, n, seed=0)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
+    peak, peak_kind = load_peaks()
+    traffic = load_traffic()
+    names = ["xinv", "zstep", "xfwd"]
+
+    # ---- plain FP64 ----
+    sim, w, dw, step = make_run(n, "double", device, w0)
+    for _ in range(args.warmup):
+        step.step()
+    torch.cuda.synchronize()
+    barrier(dist)
+    torch.cuda.synchronize()
+    t_wall0 = time.perf_counter()
+    with ClockSampler(local) as clocks:
+        per_step, per_kernel = timed_steps(step, args.steps, flush)
+    torch.cuda.synchronize()
+    barrier(dist)
+    wall = time.perf_counter() - t_wall0
+    secs = sum(per_step) * 1e-3
+    max_secs = reduce_max(secs, dist, device)
+    value = aggregate_throughput(n * n, args.steps, world, max_secs)
+    model = kernel_model(n, False)
+    roof, kdom = roofline(model, per_kernel, names, peak, peak_kind, traffic, "double")
+    avg_k = [statistics.mean(v) for v in per_kernel]
+    flops = [model[k]["flops"] for k in names]
+    fp64 = {
+        "kernel": names[kdom], "achieved_tflops": round(flops[kdom] / (avg_k[kdom] * 1e-3) / 1e12, 4),
+        "peak_tflops": FP64_FMA_TFLOPS, "frac": round(flops[kdom] / (avg_k[kdom] * 1e-3) / 1e12 / FP64_FMA_TFLOPS, 4),
+        "note": "nominal 5 N log2 N flops per complex FFT; peak = measured FP64 FMA rate of this GB300",
+    }
+
+    # ---- end to end through the public API with host buffers ----
+    h_w = torch.empty_like(w._sdata, device="cpu").pin_memory()
+    h_dw = torch.empty_like(dw._data, device="cpu").pin_memory()
+    h_w.copy_(w._sdata)
+    h_dw.copy_(dw._data)
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        w._sdata.copy_(h_w, non_blocking=True)
+        dw._data.copy_(h_dw, non_blocking=True)
+        step.step()
+        h_w.copy_(w._sdata, non_blocking=True)
+        h_dw.copy_(dw._data, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        e2e_ms.append(e0.elapsed_time(e1))
+    e2e_secs = reduce_max(sum(e2e_ms) * 1e-3, dist, device)
+    io_bytes = (h_w.numel() + h_dw.numel()) * 16
+
+    # ---- split precision ----
+    sim_s, w_s, dw_s, step_s = make_run(n, "split", device, w0)
+    for _ in range(args.warmup):
+        step_s.step()
+    torch.cuda.synchronize()
+    per_step_s, per_kernel_s = timed_steps(step_s, args.steps, flush)
+    secs_s = reduce_max(sum(per_step_s) * 1e-3, dist, device)
+    value_s = aggregate_throughput(n * n, args.steps, world, secs_s)
+    roof_s, _ = roofline(kernel_model(n, True), per_kernel_s, names, peak, peak_kind, traffic, "split")
+
+    # ---- split-precision error against the FP64 path (same initial field) ----
+    acc = {}
+    if rank == 0:
+        _, wa, _, sa = make_run(n, "double", device, w0)
+        _, wb, _, sb = make_run(n, "split", device, w0)
+        ke_a, ke_b = [], []
+        for k in range(1, 101):
+            da = sa.step(diagnostics=True)
+            db = sb.step(diagnostics=True)
+            ke_a.append(float(da[0]))
+            ke_b.append(float(db[0]))
+            if k in (1, 100):
+                err = (torch.linalg.vector_norm(wa._sdata - wb._sdata) / torch.linalg.vector_norm(wa._sdata)).item()
+                acc[f"rel_l2_{k}step" + ("s" if k > 1 else "")] = err
+        ke_a, ke_b = np.array(ke_a), np.array(ke_b)
+        acc["ke_traj_max_rel_err"] = float(np.max(np.abs(ke_b - ke_a) / np.abs(ke_a)))
+
+    # ---- CPU baseline (rank 0, N = 1 only) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cv, csecs = cpu_step_sample(w0, n, 2)
+        cpu = {"value": round(cv, 4), "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"2 timesteps at {n}x{n} after one warm step ({csecs:.1f} s), NumPy oracle on one host "
+                         "core (pocketfft is single-threaded)"}
+
+    if rank == 0:
+        ms = max_secs / args.steps * 1e3
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": DATA,
+            "config": dict(WORKLOAD, nx=n, nz=n, l2="flushed (256 MiB write) between timed steps",
+                           replicas=world),
+            "roofline": roof,
+            "fp64_alu_roof": fp64,
+            "e2e": {"value": round(aggregate_throughput(n * n, args.steps, world, e2e_secs), 3), "unit": UNIT,
+                    "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
+                    "path": "Stepper.step with state and history copied from/to pinned host memory each step"},
+            "split": {"value": round(value_s, 3), "unit": UNIT, "dtype": "f32 transforms / f64 state",
+                      "ms_per_step": round(secs_s / args.steps * 1e3, 4),
+                      "speedup_vs_fp64": round(value_s / value, 3), "roofline": roof_s, **acc},
+            "cpu_baseline": cpu,
+            "gpu_launches": step.kernel_count() * args.steps * 2,
+            "clocks": clocks.summary(),
+            "wall_s_fp64_timed": round(wall, 3),
+        }
+        print(json.dumps(line), flush=True)
+    barrier(dist)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["native", "reference"], default="native")
+    ap.add_argument("--n", type=int, default=2048, help="grid points per side (default 2048)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args(argv)
+    if args.warmup < 3 and args.impl == "native":
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_native(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,230 @@
+/* melvin_gb300.h -- C ABI of the GB300 (sm_103a) kernels behind the Melvin.py
+ * per-timestep hot path.
+ *
+ * Every entry point takes plain pointers and sizes.  Unless stated
+ * otherwise, array arguments are DEVICE pointers:
+ *   - spectral arrays are interleaved complex128 (re, im pairs of double),
+ *     row-major with the reference's spectral shape: (2nn+1, nm) when fully
+ *     spectral, (nn, nz) for Fourier-x / finite-difference-z
+ *     (melvin/Parameters.py:72-79, melvin/ArrayFactory.py:28-45);
+ *   - physical arrays are float64, row-major (nx, nz), z contiguous
+ *     (melvin/ArrayFactory.py:47-62);
+ *   - derivative histories are the reference's TimeDerivative buffer,
+ *     complex128 of shape (order, *spectral_shape) (melvin/TimeDerivative.py:13-20);
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream);
+ *   - `work` is caller-owned device scratch of at least the size returned
+ *     by mgb_workspace_bytes for the same call family.
+ * Work is enqueued asynchronously on `stream`.  Every function returns an
+ * mgb_status; mgb_last_error() gives a one-line description of the most
+ * recent failure on the calling thread.  Citations are to Melvin.py source
+ * files relative to that project's root.
+ */
+#ifndef MELVIN_GB300_H
+#define MELVIN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mgb_status {
+  MGB_OK = 0,
+  MGB_ERR_INVALID = 1,     /* bad argument (null pointer, shape, option) */
+  MGB_ERR_UNSUPPORTED = 2, /* valid for the reference, not built here (e.g. non power-of-two FFT length) */
+  MGB_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  MGB_ERR_NONFINITE = 4,   /* NaN / Inf met by a checked reduction */
+  MGB_ERR_CFL = 5,         /* CFL condition breached (melvin/Integrator.py:35-44) */
+  MGB_ERR_NOMEM = 6        /* admission / allocation refused */
+} mgb_status;
+
+typedef enum mgb_precision {
+  MGB_PREC_DOUBLE = 0, /* FP64 transforms, derivatives and products */
+  MGB_PREC_SPLIT = 1   /* FP32 transforms/derivatives/products, FP64 state, history and solves */
+} mgb_precision;
+
+/* Grid and discretisation, the subset of Parameters the path depends on
+ * (melvin/Parameters.py:9-30, 63-92). */
+typedef struct mgb_grid {
+  int32_t nx, nz;   /* physical points */
+  double lx, lz;    /* box lengths; dx = lx/nx, dz = lz/nz */
+  int32_t fdm_z;    /* 0: discretisation ["spectral","spectral"]; 1: ["spectral","fdm"] */
+  int32_t sdo;      /* spatial_derivative_order: 2 or 4 */
+  int32_t precision;/* mgb_precision */
+} mgb_grid;
+
+typedef struct mgb_plan mgb_plan;
+
+/* Spectral derivative kinds for mgb_spectral_derivative. */
+typedef enum mgb_deriv {
+  MGB_DDX = 0,   /* Variable.sddx   melvin/SpatialDifferentiator.py:50-53 */
+  MGB_DDZ = 1,   /* Variable.sddz   :55-58 (FDM-z: pddz on the spectral array, :36-40) */
+  MGB_D2DX2 = 2, /* Variable.sd2dx2 :60-63 */
+  MGB_D2DZ2 = 3, /* Variable.sd2dz2 :65-68 (FDM-z: pd2dz2, :106-128) */
+  MGB_NABLA2 = 4 /* Variable.snabla2 melvin/Variable.py:111-113 */
+} mgb_deriv;
+
+/* ---- plans ------------------------------------------------------------- */
+
+/* Validate the grid, upload twiddle tables and (FDM-z) the tridiagonal
+ * factors.  Replaces the set-up done by Simulation.__init__ and
+ * Simulation.init_laplacian_solver (melvin/Simulation.py:19-50, 67-74,
+ * melvin/LaplacianSolver.py:7-56).  Requires a power-of-two nx (and nz when
+ * fully spectral), 16 <= n <= 4096; nz >= 5 for FDM-z. */
+int mgb_plan_create(const mgb_grid* grid, mgb_plan** out);
+int mgb_plan_destroy(mgb_plan* plan);
+/* Spectral (rows, cols) and physical (nx, nz) shapes of the plan. */
+int mgb_plan_shapes(const mgb_plan* plan, int32_t* spec_rows, int32_t* spec_cols,
+                    int32_t* phys_rows, int32_t* phys_cols);
+/* Scratch bytes: family 0 = per-verb transforms, family 1 = fused step with
+ * `nfields` advected fields. */
+int mgb_workspace_bytes(const mgb_plan* plan, int32_t family, int32_t nfields, size_t* bytes);
+const char* mgb_status_string(int32_t status);
+const char* mgb_last_error(void);
+
+/* ---- transforms (melvin/SpectralTransformer.py) ------------------------- */
+
+/* Spectral -> physical: SpectralTransformer.to_physical, fully spectral
+ * (:90-150) or x-only (:33-61). */
+int mgb_to_physical(const mgb_plan* plan, const void* spec, double* phys, void* work, void* stream);
+/* Physical -> spectral: SpectralTransformer.to_spectral (:152-199, :63-88). */
+int mgb_to_spectral(const mgb_plan* plan, const double* phys, void* spec, void* work, void* stream);
+
+/* ---- derivatives (melvin/SpatialDifferentiator.py) ---------------------- */
+
+/* Central finite-difference d/dx of a physical field, x periodic
+ * (pddx, :76-89 order 2, :130-155 order 4). */
+int mgb_pddx(const mgb_plan* plan, const double* in, double* out, void* stream);
+/* Central finite-difference d/dz of a physical field, periodic when z is
+ * spectral, Dirichlet (outer points left 0) when z is FDM (pddz, :91-104,
+ * :157-185). */
+int mgb_pddz(const mgb_plan* plan, const double* in, double* out, void* stream);
+/* Spectral derivative verbs; `in` and `out` are spectral arrays. */
+int mgb_spectral_derivative(const mgb_plan* plan, int32_t kind, const void* in, void* out, void* stream);
+/* calc_lap (:70-74): real (rows, cols) array d2x*n^2 + d2z*m^2 (fully spectral). */
+int mgb_laplacian(const mgb_plan* plan, double* lap, void* stream);
+
+/* ---- streamfunction inversion (melvin/LaplacianSolver.py) -------------- */
+
+/* Solve lap(out) = rhs: spectral divide with lap(0,0) := 1 (:58-68) or the
+ * per-mode Dirichlet tridiagonal systems (:21-56, 70-79). */
+int mgb_poisson_solve(const mgb_plan* plan, const void* rhs, void* out, void* stream);
+
+/* ---- nonlinear term and velocity --------------------------------------- */
+
+/* Variable.vec_dot_nabla (melvin/Variable.py:119-128): writes q_phys =
+ * to_physical(q_spec) and out_spec = to_spectral(pddx(ux*q) + pddz(uz*q)). */
+int mgb_vec_dot_nabla(const mgb_plan* plan, const void* q_spec, double* q_phys,
+                      const double* ux, const double* uz, void* out_spec, void* work,
+                      void* stream);
+/* calc_velocity_from_vorticity (melvin/utility.py:62-79): psi = solve(-w);
+ * uz_spec = sddx(psi) and uz_phys = to_physical(uz_spec); fully spectral:
+ * ux_spec = -sddz(psi), ux_phys = to_physical(ux_spec); FDM-z: psi_phys =
+ * to_physical(psi), ux_phys = -pddz(psi_phys) (ux_spec untouched and may be
+ * NULL; psi_phys may be NULL, then scratch holds it). */
+int mgb_velocity_from_vorticity(const mgb_plan* plan, const void* w_spec, void* psi_spec,
+                                void* ux_spec, void* uz_spec, double* psi_phys,
+                                double* ux_phys, double* uz_phys, void* work, void* stream);
+
+/* ---- time integration (melvin/Integrator.py) --------------------------- */
+
+/* _semi_implicit_spectral (:58-63): var = ((1+(1-a)dt L) var + AB(hist)) /
+ * (1 - a dt L), L = lin_op (real, spectral shape); the caller advances
+ * curr.  `order` 2 or 4, `curr` = TimeDerivative._curr_idx. */
+int mgb_integrate_semi_implicit(const mgb_plan* plan, void* var, void* hist, int32_t order,
+                                int32_t curr, double dt, double alpha, const double* lin_op,
+                                void* stream);
+/* _explicit (:53-56): hist[curr] += diffusion; var += AB(hist). */
+int mgb_integrate_explicit(const mgb_plan* plan, void* var, void* hist, int32_t order,
+                           int32_t curr, double dt, const void* diffusion, void* stream);
+/* Predictor (corrector=0: AB2/AB4, :5-18) or corrector (corrector=1:
+ * AM2/AM4, :20-33) value written to `out`. */
+int mgb_adams(const mgb_plan* plan, int32_t corrector, const void* hist, int32_t order,
+              int32_t curr, double dt, void* out, void* stream);
+
+/* ---- diagnostics ------------------------------------------------------- */
+
+/* Device reductions over physical ux, uz (deterministic order):
+ * out[0] = calc_kinetic_energy (melvin/utility.py:42-59),
+ * out[1] = max(ux), out[2] = max(uz) (signed maxima used by
+ * Integrator.set_dt, melvin/Integrator.py:35-44).  `out` is device memory
+ * of 3 doubles; `work` needs mgb_workspace_bytes(family 0). */
+int mgb_diagnostics(const mgb_plan* plan, const double* ux, const double* uz, double* out,
+                    void* work, void* stream);
+
+/* ---- fused timestep ---------------------------------------------------- */
+
+/* One linear term of an advected field's right-hand side:
+ * rhs += coef * op(src), op 0 = value, 1 = d/dx (i kx), 2 = d/dz (i kz);
+ * src = field index, or -1 for the streamfunction psi = solve(-field 0).
+ * E.g. `- params.Pr * params.Ra * tmp.sddx()`
+ * (examples/rayleigh_benard_convection.py:102-105) is {src=T, op=1,
+ * coef=-Pr*Ra}; `- uz[:]` (examples/double_diffusive_convection.py:115) is
+ * {src=-1, op=1, coef=-1}. */
+typedef struct mgb_term {
+  int32_t src;
+  int32_t op;
+  double coef;
+} mgb_term;
+
+/* Boundary/mean rules applied after the update (bit flags). */
+enum {
+  MGB_BC_ZERO_M0 = 1,      /* field[:, 0] = 0  (examples/double_diffusive_convection.py:122-124) */
+  MGB_BC_DIRICHLET_W = 2,  /* FDM-z vorticity rows: w[1:, edges] = 0, w[0, :] = 0
+                              (examples/rayleigh_benard_convection.py:112-142) */
+  MGB_BC_DIRICHLET_T = 4   /* FDM-z scalar: t[0, lower edge] = 1, t[0, upper edge] = 0,
+                              t[1:, edges] = 0 (same lines) */
+};
+
+typedef struct mgb_field_eq {
+  double kappa;        /* diffusion coefficient: lin_op = kappa * lap */
+  int32_t nterms;      /* <= 4 */
+  mgb_term terms[4];
+  int32_t bc;          /* MGB_BC_* flags */
+} mgb_field_eq;
+
+enum {
+  MGB_INT_SEMI_IMPLICIT = 0, /* Integrator._semi_implicit_spectral (fully spectral only) */
+  MGB_INT_EXPLICIT = 1,      /* Integrator._explicit */
+  MGB_INT_PECE = 2           /* AB predictor, re-evaluation, AM corrector (defined here;
+                                the reference defines the AM formulae but never calls them) */
+};
+
+/* The equation set of one user loop body: field 0 is the vorticity, the
+ * others are scalars advected by the same velocity. */
+typedef struct mgb_equation {
+  int32_t nfields;     /* 1..3 */
+  int32_t integrator;  /* MGB_INT_* */
+  int32_t order;       /* integrator_order: 2 or 4 */
+  double alpha;        /* semi-implicit alpha (Parameters.alpha = 0.51) */
+  mgb_field_eq f[3];
+} mgb_equation;
+
+/* One timestep of the whole loop body (velocity from vorticity, nonlinear
+ * terms, linear terms, update, boundary rules) for `eq`, fused into a few
+ * kernels.  q[f]: spectral states (updated in place); hist[f]: histories;
+ * `curr` is the history slot that receives this step's derivative (the
+ * caller advances it afterwards, as TimeDerivative.advance does).  `diag`
+ * (device, 3 doubles, may be NULL) receives kinetic energy, max ux, max uz
+ * of the velocity at the start of the step. */
+int mgb_step(const mgb_plan* plan, const mgb_equation* eq, void* const* q, void* const* hist,
+             int32_t curr, double dt, void* work, double* diag, void* stream);
+
+/* Number of kernels one mgb_step launches for `eq` on this plan (not
+ * counting the diagnostics fold): 3 fully spectral, 4 FDM-z explicit, 8
+ * FDM-z predictor-corrector.  No reference counterpart (instrumentation). */
+int mgb_step_kernel_count(const mgb_plan* plan, const mgb_equation* eq, int32_t* count);
+/* mgb_step that also records caller-created CUDA events on `stream`:
+ * events[0] before the first kernel and events[k] after kernel k, for
+ * k < nevents (count+1 events time every kernel).  No reference
+ * counterpart (instrumentation for per-kernel rooflines). */
+int mgb_step_events(const mgb_plan* plan, const mgb_equation* eq, void* const* q, void* const* hist,
+                    int32_t curr, double dt, void* work, double* diag, void* stream,
+                    void* const* events, int32_t nevents);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MELVIN_GB300_H */

@@ -1,0 +1,360 @@
+// The extern "C" entry points declared in include/melvin_gb300.h.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <new>
+#include <vector>
+
+#include "internal.h"
+
+namespace mgb {
+
+static thread_local char g_last_error[512] = "";
+
+int fail(int status, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+  return status;
+}
+
+int cuda_check(cudaError_t e, const char* what) {
+  return fail(MGB_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+static bool pow2_in_range(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; }
+
+// exp(-2*pi*i*t/n), t in [0, n), evaluated in long double; the values on the
+// axes are exact.
+static void twiddles(int n, std::vector<double>& d, std::vector<float>& f) {
+  d.resize(2 * (size_t)n);
+  f.resize(2 * (size_t)n);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int t = 0; t < n; ++t) {
+    long double c, s;
+    if (t == 0) {
+      c = 1.0L, s = 0.0L;
+    } else if (4 * t == n) {
+      c = 0.0L, s = 1.0L;
+    } else if (2 * t == n) {
+      c = -1.0L, s = 0.0L;
+    } else if (4 * t == 3 * n) {
+      c = 0.0L, s = -1.0L;
+    } else {
+      const long double ang = 2.0L * pi * (long double)t / (long double)n;
+      c = cosl(ang);
+      s = sinl(ang);
+    }
+    d[2 * t] = (double)c;
+    d[2 * t + 1] = (double)(-s);
+    f[2 * t] = (float)c;
+    f[2 * t + 1] = (float)(-s);
+  }
+}
+
+static int upload_twiddles(int n, void** td, void** tf) {
+  std::vector<double> d;
+  std::vector<float> f;
+  twiddles(n, d, f);
+  MGB_CUDA(cudaMalloc(td, d.size() * sizeof(double)));
+  MGB_CUDA(cudaMalloc(tf, f.size() * sizeof(float)));
+  MGB_CUDA(cudaMemcpy(*td, d.data(), d.size() * sizeof(double), cudaMemcpyHostToDevice));
+  MGB_CUDA(cudaMemcpy(*tf, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return MGB_OK;
+}
+
+static void release(mgb_plan* p) {
+  if (!p) return;
+  cudaFree(p->tw_x_d);
+  cudaFree(p->tw_x_f);
+  cudaFree(p->tw_z_d);
+  cudaFree(p->tw_z_f);
+  cudaFree(p->th_inv);
+  cudaFree(p->th_cp);
+  delete p;
+}
+
+}  // namespace mgb
+
+using namespace mgb;
+
+#define CHECK_PLAN(p) \
+  if (!(p)) return fail(MGB_ERR_INVALID, "%s: null plan", __func__)
+#define CHECK_PTR(x) \
+  if (!(x)) return fail(MGB_ERR_INVALID, "%s: null pointer '%s'", __func__, #x)
+
+extern "C" {
+
+const char* mgb_last_error(void) { return g_last_error; }
+
+const char* mgb_status_string(int32_t status) {
+  switch (status) {
+    case MGB_OK: return "ok";
+    case MGB_ERR_INVALID: return "invalid argument";
+    case MGB_ERR_UNSUPPORTED: return "unsupported configuration";
+    case MGB_ERR_CUDA: return "CUDA error";
+    case MGB_ERR_NONFINITE: return "non-finite value";
+    case MGB_ERR_CFL: return "CFL condition breached";
+    case MGB_ERR_NOMEM: return "out of device memory";
+    default: return "unknown status";
+  }
+}
+
+int mgb_plan_create(const mgb_grid* grid, mgb_plan** out) {
+  CHECK_PTR(grid);
+  CHECK_PTR(out);
+  *out = nullptr;
+  const mgb_grid& G = *grid;
+  if (!pow2_in_range(G.nx))
+    return fail(MGB_ERR_UNSUPPORTED, "nx=%d: x transforms need a power of two in [16, 4096]", G.nx);
+  if (!G.fdm_z && !pow2_in_range(G.nz))
+    return fail(MGB_ERR_UNSUPPORTED, "nz=%d: fully spectral z transforms need a power of two in [16, 4096]", G.nz);
+  if (G.fdm_z && (G.nz < 5 || G.nz > 1800))
+    return fail(MGB_ERR_UNSUPPORTED, "nz=%d: FDM z axis needs 5 <= nz <= 1800", G.nz);
+  if (G.sdo != 2 && G.sdo != 4)
+    return fail(MGB_ERR_INVALID, "spatial_derivative_order=%d (2 or 4)", G.sdo);
+  if (G.precision != MGB_PREC_DOUBLE && G.precision != MGB_PREC_SPLIT)
+    return fail(MGB_ERR_INVALID, "precision=%d", G.precision);
+  if (!(G.lx > 0) || !(G.lz > 0)) return fail(MGB_ERR_INVALID, "box lengths must be positive");
+  mgb_plan* p = new (std::nothrow) mgb_plan();
+  if (!p) return fail(MGB_ERR_NOMEM, "plan allocation");
+  p->grid = G;
+  GridC& g = p->g;
+  g.nx = G.nx;
+  g.nz = G.nz;
+  g.nn = (G.nx - 1) / 3;
+  g.fdm = G.fdm_z ? 1 : 0;
+  g.nm = G.fdm_z ? G.nz : (G.nz - 1) / 3;
+  g.rows = G.fdm_z ? g.nn : 2 * g.nn + 1;
+  g.cols = g.nm;
+  g.sdo = G.sdo;
+  g.dx = G.lx / G.nx;
+  g.dz = G.lz / G.nz;
+  const double tp = 2.0 * M_PI;
+  g.dfx = tp / G.lx;
+  g.dfz = tp / G.lz;
+  g.d2x = -((tp * tp) / (G.lx * G.lx));
+  g.d2z = -((tp * tp) / (G.lz * G.lz));
+  cudaGetDevice(&p->device);
+  int st = upload_twiddles(G.nx, &p->tw_x_d, &p->tw_x_f);
+  if (!st && !G.fdm_z) st = upload_twiddles(G.nz, &p->tw_z_d, &p->tw_z_f);
+  if (!st && G.fdm_z) st = fd_plan_init(p);
+  if (st) {
+    release(p);
+    return st;
+  }
+  *out = p;
+  return MGB_OK;
+}
+
+int mgb_plan_destroy(mgb_plan* plan) {
+  release(plan);
+  return MGB_OK;
+}
+
+int mgb_plan_shapes(const mgb_plan* p, int32_t* spec_rows, int32_t* spec_cols, int32_t* phys_rows,
+                    int32_t* phys_cols) {
+  CHECK_PLAN(p);
+  if (spec_rows) *spec_rows = p->g.rows;
+  if (spec_cols) *spec_cols = p->g.cols;
+  if (phys_rows) *phys_rows = p->g.nx;
+  if (phys_cols) *phys_cols = p->g.nz;
+  return MGB_OK;
+}
+
+int mgb_workspace_bytes(const mgb_plan* p, int32_t family, int32_t nfields, size_t* bytes) {
+  CHECK_PLAN(p);
+  CHECK_PTR(bytes);
+  const size_t diag = 152 * 4 * 3 * sizeof(double) + 256;
+  if (family == 0) {
+    size_t b = p->g.fdm ? fd_verb_workspace(p) : 2 * inter_bytes(p->g, false);
+    *bytes = (b > diag ? b : diag) + 256;
+    return MGB_OK;
+  }
+  if (family == 1) {
+    if (nfields < 1 || nfields > 3) return fail(MGB_ERR_INVALID, "nfields=%d (1..3)", nfields);
+    *bytes = (p->g.fdm ? fd_step_workspace(p, nfields) : fs_step_workspace(p, nfields)) + 256;
+    return MGB_OK;
+  }
+  return fail(MGB_ERR_INVALID, "workspace family %d", family);
+}
+
+int mgb_to_physical(const mgb_plan* p, const void* spec, double* phys, void* work, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(spec);
+  CHECK_PTR(phys);
+  if (p->g.fdm) return fd_to_physical(p, (const zd*)spec, phys, (cudaStream_t)stream);
+  CHECK_PTR(work);
+  return fs_to_physical(p, (const zd*)spec, phys, work, (cudaStream_t)stream);
+}
+
+int mgb_to_spectral(const mgb_plan* p, const double* phys, void* spec, void* work, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(spec);
+  CHECK_PTR(phys);
+  if (p->g.fdm) return fd_to_spectral(p, phys, (zd*)spec, (cudaStream_t)stream);
+  CHECK_PTR(work);
+  return fs_to_spectral(p, phys, (zd*)spec, work, (cudaStream_t)stream);
+}
+
+int mgb_pddx(const mgb_plan* p, const double* in, double* out, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(in);
+  CHECK_PTR(out);
+  if (in == out) return fail(MGB_ERR_INVALID, "pddx: input and output must differ");
+  return pw_pddx(p, in, out, (cudaStream_t)stream);
+}
+
+int mgb_pddz(const mgb_plan* p, const double* in, double* out, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(in);
+  CHECK_PTR(out);
+  if (in == out) return fail(MGB_ERR_INVALID, "pddz: input and output must differ");
+  return pw_pddz(p, in, out, (cudaStream_t)stream);
+}
+
+int mgb_spectral_derivative(const mgb_plan* p, int32_t kind, const void* in, void* out, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(in);
+  CHECK_PTR(out);
+  return pw_spectral_derivative(p, kind, (const zd*)in, (zd*)out, (cudaStream_t)stream);
+}
+
+int mgb_laplacian(const mgb_plan* p, double* lap, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(lap);
+  return pw_laplacian(p, lap, (cudaStream_t)stream);
+}
+
+int mgb_poisson_solve(const mgb_plan* p, const void* rhs, void* out, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(rhs);
+  CHECK_PTR(out);
+  if (p->g.fdm) return fd_poisson(p, (const zd*)rhs, (zd*)out, (cudaStream_t)stream);
+  return pw_poisson_spectral(p, (const zd*)rhs, (zd*)out, (cudaStream_t)stream);
+}
+
+int mgb_vec_dot_nabla(const mgb_plan* p, const void* q_spec, double* q_phys, const double* ux, const double* uz,
+                      void* out_spec, void* work, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(q_spec);
+  CHECK_PTR(q_phys);
+  CHECK_PTR(ux);
+  CHECK_PTR(uz);
+  CHECK_PTR(out_spec);
+  CHECK_PTR(work);
+  if (p->g.fdm)
+    return fd_vec_dot_nabla(p, (const zd*)q_spec, q_phys, ux, uz, (zd*)out_spec, work, (cudaStream_t)stream);
+  return fs_vec_dot_nabla(p, (const zd*)q_spec, q_phys, ux, uz, (zd*)out_spec, work, (cudaStream_t)stream);
+}
+
+int mgb_velocity_from_vorticity(const mgb_plan* p, const void* w_spec, void* psi_spec, void* ux_spec, void* uz_spec,
+                                double* psi_phys, double* ux_phys, double* uz_phys, void* work, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(w_spec);
+  CHECK_PTR(psi_spec);
+  CHECK_PTR(ux_phys);
+  CHECK_PTR(uz_phys);
+  CHECK_PTR(work);
+  if (p->g.fdm)
+    return fd_velocity(p, (const zd*)w_spec, (zd*)psi_spec, (zd*)uz_spec, psi_phys, ux_phys, uz_phys, work,
+                       (cudaStream_t)stream);
+  return fs_velocity(p, (const zd*)w_spec, (zd*)psi_spec, (zd*)ux_spec, (zd*)uz_spec, ux_phys, uz_phys, work,
+                     (cudaStream_t)stream);
+}
+
+int mgb_integrate_semi_implicit(const mgb_plan* p, void* var, void* hist, int32_t order, int32_t curr, double dt,
+                                double alpha, const double* lin_op, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(var);
+  CHECK_PTR(hist);
+  CHECK_PTR(lin_op);
+  if (order != 2 && order != 4) return fail(MGB_ERR_INVALID, "integrator_order=%d (2 or 4)", order);
+  if (curr < 0 || curr >= order) return fail(MGB_ERR_INVALID, "curr_idx=%d out of range", curr);
+  return pw_integrate_semi_implicit(p, (zd*)var, (zd*)hist, order, curr, dt, alpha, lin_op, (cudaStream_t)stream);
+}
+
+int mgb_integrate_explicit(const mgb_plan* p, void* var, void* hist, int32_t order, int32_t curr, double dt,
+                           const void* diffusion, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(var);
+  CHECK_PTR(hist);
+  CHECK_PTR(diffusion);
+  if (order != 2 && order != 4) return fail(MGB_ERR_INVALID, "integrator_order=%d (2 or 4)", order);
+  if (curr < 0 || curr >= order) return fail(MGB_ERR_INVALID, "curr_idx=%d out of range", curr);
+  return pw_integrate_explicit(p, (zd*)var, (zd*)hist, order, curr, dt, (const zd*)diffusion, (cudaStream_t)stream);
+}
+
+int mgb_adams(const mgb_plan* p, int32_t corrector, const void* hist, int32_t order, int32_t curr, double dt,
+              void* out, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(hist);
+  CHECK_PTR(out);
+  if (order != 2 && order != 4) return fail(MGB_ERR_INVALID, "integrator_order=%d (2 or 4)", order);
+  if (curr < 0 || curr >= order) return fail(MGB_ERR_INVALID, "curr_idx=%d out of range", curr);
+  return pw_adams(p, corrector, (const zd*)hist, order, curr, dt, (zd*)out, (cudaStream_t)stream);
+}
+
+int mgb_diagnostics(const mgb_plan* p, const double* ux, const double* uz, double* out, void* work, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(ux);
+  CHECK_PTR(uz);
+  CHECK_PTR(out);
+  CHECK_PTR(work);
+  return pw_diagnostics(p, ux, uz, out, work, (cudaStream_t)stream);
+}
+
+static int step_impl(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist, int32_t curr,
+                     double dt, void* work, double* diag, void* stream, EventTrack* et) {
+  CHECK_PLAN(p);
+  CHECK_PTR(eq);
+  CHECK_PTR(q);
+  CHECK_PTR(hist);
+  CHECK_PTR(work);
+  const int F = eq->nfields;
+  if (F < 1 || F > 3) return fail(MGB_ERR_INVALID, "nfields=%d (1..3)", F);
+  if (eq->order != 2 && eq->order != 4) return fail(MGB_ERR_INVALID, "integrator_order=%d (2 or 4)", eq->order);
+  if (curr < 0 || curr >= eq->order) return fail(MGB_ERR_INVALID, "curr_idx=%d out of range", curr);
+  for (int f = 0; f < F; ++f) {
+    if (!q[f] || !hist[f]) return fail(MGB_ERR_INVALID, "null state or history for field %d", f);
+    const mgb_field_eq& fe = eq->f[f];
+    if (fe.nterms < 0 || fe.nterms > 4) return fail(MGB_ERR_INVALID, "field %d: nterms=%d (0..4)", f, fe.nterms);
+    for (int t = 0; t < fe.nterms; ++t) {
+      if (fe.terms[t].src < -1 || fe.terms[t].src >= F)
+        return fail(MGB_ERR_INVALID, "field %d term %d: src=%d", f, t, fe.terms[t].src);
+      if (fe.terms[t].op < 0 || fe.terms[t].op > 2)
+        return fail(MGB_ERR_INVALID, "field %d term %d: op=%d", f, t, fe.terms[t].op);
+    }
+  }
+  if (p->g.fdm) return fd_step(p, eq, q, hist, curr, dt, work, diag, (cudaStream_t)stream, et);
+  if (eq->integrator != MGB_INT_SEMI_IMPLICIT && eq->integrator != MGB_INT_EXPLICIT)
+    return fail(MGB_ERR_UNSUPPORTED, "fully spectral step: integrator %d", eq->integrator);
+  return fs_step(p, eq, q, hist, curr, dt, work, diag, (cudaStream_t)stream, et);
+}
+
+int mgb_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist, int32_t curr, double dt,
+             void* work, double* diag, void* stream) {
+  return step_impl(p, eq, q, hist, curr, dt, work, diag, stream, nullptr);
+}
+
+int mgb_step_kernel_count(const mgb_plan* p, const mgb_equation* eq, int32_t* count) {
+  CHECK_PLAN(p);
+  CHECK_PTR(eq);
+  CHECK_PTR(count);
+  if (!p->g.fdm) *count = 3;
+  else *count = eq->integrator == MGB_INT_PECE ? 8 : 4;
+  return MGB_OK;
+}
+
+int mgb_step_events(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist, int32_t curr,
+                    double dt, void* work, double* diag, void* stream, void* const* events, int32_t nevents) {
+  CHECK_PTR(events);
+  EventTrack et;
+  et.ev = (cudaEvent_t*)events;
+  et.nev = nevents;
+  return step_impl(p, eq, q, hist, curr, dt, work, diag, stream, &et);
+}
+
+}  // extern "C"

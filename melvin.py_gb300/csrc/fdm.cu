@@ -1,0 +1,351 @@
+// Host orchestration of the Fourier-x / Dirichlet-z kernels, plus the two
+// small physical stencil kernels of the per-verb API.
+#include <vector>
+
+#include "fdm_impl.cuh"
+
+namespace mgb {
+
+const FdLaunchers* fd_launchers_16();
+const FdLaunchers* fd_launchers_32();
+const FdLaunchers* fd_launchers_64();
+const FdLaunchers* fd_launchers_128();
+const FdLaunchers* fd_launchers_256();
+const FdLaunchers* fd_launchers_512();
+const FdLaunchers* fd_launchers_1024();
+const FdLaunchers* fd_launchers_2048();
+const FdLaunchers* fd_launchers_4096();
+
+const FdLaunchers* fd_launchers(int N) {
+  switch (N) {
+    case 16: return fd_launchers_16();
+    case 32: return fd_launchers_32();
+    case 64: return fd_launchers_64();
+    case 128: return fd_launchers_128();
+    case 256: return fd_launchers_256();
+    case 512: return fd_launchers_512();
+    case 1024: return fd_launchers_1024();
+    case 2048: return fd_launchers_2048();
+    case 4096: return fd_launchers_4096();
+    default: return nullptr;
+  }
+}
+
+namespace {
+
+inline double fd_inv(int sdo, double h) { return sdo == 2 ? 1.0 / (2.0 * h) : 1.0 / (3.0 * h); }
+
+int launched(cudaError_t e, const char* what) {
+  if (e == cudaErrorInvalidConfiguration)
+    return fail(MGB_ERR_UNSUPPORTED, "%s: shared-memory footprint too large for this size", what);
+  if (e != cudaSuccess) return cuda_check(e, what);
+  return MGB_OK;
+}
+
+inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// ux = -pddz(psi) on the physical streamfunction, Dirichlet z
+// (melvin/utility.py:66-69).
+__global__ void k_fd_vel(GridC g, const double* __restrict__ psi, double* __restrict__ ux, double fdz) {
+  const size_t total = (size_t)g.nx * g.nz;
+  const int h = g.sdo / 2;
+  for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < total; i += (size_t)gridDim.x * NT) {
+    const int x = (int)(i / g.nz), z = (int)(i - (size_t)x * g.nz);
+    const double* row = psi + (size_t)x * g.nz;
+    double u = 0.0;
+    if (z >= h && z < g.nz - h)
+      u = st1(h == 2 ? row[z + 2] : 0.0, row[z + 1], row[z - 1], h == 2 ? row[z - 2] : 0.0, g.sdo, fdz);
+    ux[i] = -u;
+  }
+}
+
+// J = pddx(ux q) + pddz(uz q) with z Dirichlet (melvin/Variable.py:125-127).
+__global__ void k_fd_vdn_phys(GridC g, const double* __restrict__ q, const double* __restrict__ ux,
+                              const double* __restrict__ uz, double* __restrict__ J, double fdx, double fdz) {
+  const size_t total = (size_t)g.nx * g.nz;
+  const int h = g.sdo / 2;
+  for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < total; i += (size_t)gridDim.x * NT) {
+    const int x = (int)(i / g.nz), z = (int)(i - (size_t)x * g.nz);
+    auto px = [&](int dx) {
+      int xx = x + dx;
+      xx = xx < 0 ? xx + g.nx : (xx >= g.nx ? xx - g.nx : xx);
+      const size_t k = (size_t)xx * g.nz + z;
+      return ux[k] * q[k];
+    };
+    double jx = st1(px(2), px(1), px(-1), px(-2), g.sdo, fdx);
+    double jz = 0.0;
+    if (z >= h && z < g.nz - h) {
+      auto pz = [&](int dz) {
+        const size_t k = (size_t)x * g.nz + z + dz;
+        return uz[k] * q[k];
+      };
+      jz = st1(h == 2 ? pz(2) : 0.0, pz(1), pz(-1), h == 2 ? pz(-2) : 0.0, g.sdo, fdz);
+    }
+    J[i] = jx + jz;
+  }
+}
+
+inline int grid_for(size_t n) {
+  size_t b = (n + NT - 1) / NT;
+  return (int)(b > 152 * 16 ? 152 * 16 : (b < 1 ? 1 : b));
+}
+
+int thomas(const mgb_plan* p, const zd* rhs, double sign, zd* out, cudaStream_t s) {
+  const GridC& g = p->g;
+  const size_t smem = (size_t)TH_MODES * g.nz * sizeof(zd);
+  if (smem > kMaxDynSmem) return fail(MGB_ERR_UNSUPPORTED, "nz=%d too large for the Thomas kernel", g.nz);
+  cudaError_t e = prep_smem(k_thomas, smem);
+  if (e != cudaSuccess) return cuda_check(e, "thomas smem");
+  k_thomas<<<(g.nn + TH_MODES - 1) / TH_MODES, NT, smem, s>>>(g, rhs, sign, out, p->th_inv, p->th_cp);
+  MGB_LAUNCH_CHECK();
+  return MGB_OK;
+}
+
+}  // namespace
+
+int fd_plan_init(mgb_plan* p) {
+  const GridC& g = p->g;
+  const size_t n = (size_t)g.nn * g.nz;
+  std::vector<double> ip(n, 0.0), cp(n, 0.0);
+  const double a = 1.0 / (g.dz * g.dz);
+  const double kx = g.dfx;  // |2*pi*i/lx|
+  for (int m = 0; m < g.nn; ++m) {
+    // diagonal -((n*|ddx|)^2 + 2/dz^2), off-diagonals 1/dz^2, identity end rows
+    // (melvin/LaplacianSolver.py:25-52)
+    const double nk = (double)m * kx;
+    const double b = -(nk * nk + 2.0 / (g.dz * g.dz));
+    double* ipm = ip.data() + (size_t)m * g.nz;
+    double* cpm = cp.data() + (size_t)m * g.nz;
+    ipm[0] = 1.0;
+    cpm[0] = 0.0;
+    for (int j = 1; j < g.nz - 1; ++j) {
+      const double piv = b - a * cpm[j - 1];
+      ipm[j] = 1.0 / piv;
+      cpm[j] = a / piv;
+    }
+    ipm[g.nz - 1] = 1.0;
+    cpm[g.nz - 1] = 0.0;
+  }
+  MGB_CUDA(cudaMalloc(&p->th_inv, n * sizeof(double)));
+  MGB_CUDA(cudaMalloc(&p->th_cp, n * sizeof(double)));
+  MGB_CUDA(cudaMemcpy(p->th_inv, ip.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  MGB_CUDA(cudaMemcpy(p->th_cp, cp.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  return MGB_OK;
+}
+
+int fd_poisson(const mgb_plan* p, const zd* rhs, zd* out, cudaStream_t s) { return thomas(p, rhs, 1.0, out, s); }
+
+int fd_to_physical(const mgb_plan* p, const zd* spec, double* phys, cudaStream_t s) {
+  const GridC& g = p->g;
+  FdXinvArgs xa = {};
+  xa.g = g;
+  xa.tw = p->tw_x_d;
+  xa.job[0] = FdXinvJob{spec, phys, nullptr, 0.0, FD_COPY, nullptr};
+  return launched(fd_launchers(g.nx)->xinv[0](xa, 1, s), "fdm to_physical");
+}
+
+int fd_to_spectral(const mgb_plan* p, const double* phys, zd* spec, cudaStream_t s) {
+  const GridC& g = p->g;
+  FdXfArgs fa = {};
+  fa.g = g;
+  fa.jin[0] = phys;
+  fa.out = spec;
+  fa.nf = 1;
+  fa.mode = FD_OUT;
+  fa.inv_nx = 1.0 / (double)g.nx;
+  fa.tw = p->tw_x_d;
+  return launched(fd_launchers(g.nx)->xfwd[0][0](fa, s), "fdm to_spectral");
+}
+
+size_t fd_verb_workspace(const mgb_plan* p) {
+  return align256((size_t)p->g.nx * p->g.nz * sizeof(double)) + align256(152 * 4 * 3 * sizeof(double));
+}
+
+int fd_vec_dot_nabla(const mgb_plan* p, const zd* q, double* q_phys, const double* ux, const double* uz, zd* out,
+                     void* work, cudaStream_t s) {
+  const GridC& g = p->g;
+  int st = fd_to_physical(p, q, q_phys, s);
+  if (st) return st;
+  double* J = (double*)work;
+  k_fd_vdn_phys<<<grid_for((size_t)g.nx * g.nz), NT, 0, s>>>(g, q_phys, ux, uz, J, fd_inv(g.sdo, g.dx),
+                                                            fd_inv(g.sdo, g.dz));
+  MGB_LAUNCH_CHECK();
+  return fd_to_spectral(p, J, out, s);
+}
+
+int fd_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* uz_s, double* psi_phys, double* ux, double* uz,
+                void* work, cudaStream_t s) {
+  const GridC& g = p->g;
+  int st = thomas(p, w, -1.0, psi, s);
+  if (st) return st;
+  double* pp = psi_phys ? psi_phys : (double*)work;
+  FdXinvArgs xa = {};
+  xa.g = g;
+  xa.fdz = fd_inv(g.sdo, g.dz);
+  xa.tw = p->tw_x_d;
+  xa.job[0] = FdXinvJob{psi, pp, nullptr, 0.0, FD_COPY, nullptr};
+  xa.job[1] = FdXinvJob{psi, uz, nullptr, 0.0, FD_UZ, uz_s};
+  st = launched(fd_launchers(g.nx)->xinv[0](xa, 2, s), "fdm velocity x pass");
+  if (st) return st;
+  k_fd_vel<<<grid_for((size_t)g.nx * g.nz), NT, 0, s>>>(g, pp, ux, fd_inv(g.sdo, g.dz));
+  MGB_LAUNCH_CHECK();
+  return MGB_OK;
+}
+
+// Scratch of the fused FDM step: psi_hat, physical psi and fields, J per
+// field, predicted states (PECE), diagnostics partials.
+struct FdWork {
+  zd* psi;
+  void* phys[5];
+  void* J[3];
+  zd* qpred[3];
+  double* partial;
+  size_t bytes;
+};
+
+static FdWork fd_carve(const mgb_plan* p, int F, void* base) {
+  const GridC& g = p->g;
+  const bool split = p->grid.precision == MGB_PREC_SPLIT;
+  const size_t S = align256((size_t)g.nn * g.nz * sizeof(zd));
+  const size_t P = align256((size_t)g.nx * g.nz * (split ? sizeof(float) : sizeof(double)));
+  const int nctas = ((g.nz + FD_TZ - 1) / FD_TZ) * ((g.nx + FD_TX - 1) / FD_TX);
+  FdWork w = {};
+  char* c = (char*)base;
+  size_t off = 0;
+  w.psi = (zd*)(c + off);
+  off += S;
+  for (int i = 0; i < 2 + F; ++i) {
+    w.phys[i] = c + off;
+    off += P;
+  }
+  for (int f = 0; f < F; ++f) {
+    w.J[f] = c + off;
+    off += P;
+  }
+  for (int f = 0; f < F; ++f) {
+    w.qpred[f] = (zd*)(c + off);
+    off += S;
+  }
+  w.partial = (double*)(c + off);
+  off += align256((size_t)nctas * 3 * sizeof(double));
+  w.bytes = off;
+  return w;
+}
+
+size_t fd_step_workspace(const mgb_plan* p, int nfields) { return fd_carve(p, nfields, nullptr).bytes; }
+
+// One evaluation of the right-hand side at states `qeval` followed by the
+// update selected by `mode`.
+static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, zd* const* q, zd* const* qeval,
+                    zd* const* hist, int curr, double dt, int mode, double* diag_partial, cudaStream_t s,
+                    EventTrack* et) {
+  const GridC& g = p->g;
+  const int F = eq->nfields;
+  const int split = p->grid.precision == MGB_PREC_SPLIT ? 1 : 0;
+  const FdLaunchers* L = fd_launchers(g.nx);
+  int st = thomas(p, qeval[0], -1.0, w.psi, s);
+  if (st) return st;
+  et->mark(s);
+  FdXinvArgs xa = {};
+  xa.g = g;
+  xa.fdz = fd_inv(g.sdo, g.dz);
+  xa.tw = split ? p->tw_x_f : p->tw_x_d;
+  xa.job[0] = FdXinvJob{w.psi, w.phys[0], nullptr, 0.0, FD_UX, nullptr};
+  xa.job[1] = FdXinvJob{w.psi, w.phys[1], nullptr, 0.0, FD_UZ, nullptr};
+  for (int f = 0; f < F; ++f)
+    xa.job[2 + f] = FdXinvJob{qeval[f], w.phys[2 + f], hist[f] + (size_t)curr * g.nn * g.nz, eq->f[f].kappa,
+                              FD_COPY, nullptr};
+  st = launched(L->xinv[split](xa, 2 + F, s), "fdm step x pass");
+  if (st) return st;
+  et->mark(s);
+  FdPhysArgs pa = {};
+  pa.g = g;
+  pa.ux = w.phys[0];
+  pa.uz = w.phys[1];
+  for (int f = 0; f < F; ++f) {
+    pa.q[f] = w.phys[2 + f];
+    pa.jout[f] = w.J[f];
+  }
+  pa.nf = F;
+  pa.partial = diag_partial;
+  pa.fdx = fd_inv(g.sdo, g.dx);
+  pa.fdz = fd_inv(g.sdo, g.dz);
+  dim3 grid((g.nz + FD_TZ - 1) / FD_TZ, (g.nx + FD_TX - 1) / FD_TX);
+  if (split)
+    k_fd_phys<float><<<grid, NT, 0, s>>>(pa);
+  else
+    k_fd_phys<double><<<grid, NT, 0, s>>>(pa);
+  MGB_LAUNCH_CHECK();
+  et->mark(s);
+  FdXfArgs fa = {};
+  fa.g = g;
+  for (int f = 0; f < F; ++f) {
+    fa.jin[f] = w.J[f];
+    fa.q[f] = q[f];
+    fa.qsrc[f] = qeval[f];
+    fa.qpred[f] = w.qpred[f];
+    fa.hist[f] = hist[f];
+    const mgb_field_eq& fe = eq->f[f];
+    fa.eq[f].nterms = fe.nterms;
+    fa.eq[f].bc = fe.bc;
+    for (int t = 0; t < fe.nterms; ++t) {
+      fa.eq[f].tsrc[t] = fe.terms[t].src;
+      fa.eq[f].top[t] = fe.terms[t].op;
+      fa.eq[f].tcoef[t] = fe.terms[t].coef;
+    }
+  }
+  fa.psi = w.psi;
+  fa.nf = F;
+  fa.mode = mode;
+  fa.order = eq->order;
+  fa.curr = curr;
+  fa.dt = dt;
+  fa.inv_nx = 1.0 / (double)g.nx;
+  fa.tw = split ? p->tw_x_f : p->tw_x_d;
+  st = launched(L->xfwd[split][F - 1](fa, s), "fdm step forward x pass");
+  if (st) return st;
+  et->mark(s);
+  return MGB_OK;
+}
+
+int fd_step(const mgb_plan* p, const mgb_equation* eq, void* const* qv, void* const* hv, int curr, double dt,
+            void* work, double* diag, cudaStream_t s, EventTrack* et) {
+  EventTrack none;
+  if (!et) et = &none;
+  et->mark(s);
+  const GridC& g = p->g;
+  const int F = eq->nfields;
+  for (int f = 0; f < F; ++f)
+    for (int t = 0; t < eq->f[f].nterms; ++t)
+      if (eq->f[f].terms[t].op == 2)
+        return fail(MGB_ERR_UNSUPPORTED, "d/dz linear terms are not pointwise on an FDM z axis");
+  FdWork w = fd_carve(p, F, work);
+  zd* q[3] = {nullptr, nullptr, nullptr};
+  zd* h[3] = {nullptr, nullptr, nullptr};
+  for (int f = 0; f < F; ++f) {
+    q[f] = (zd*)qv[f];
+    h[f] = (zd*)hv[f];
+  }
+  const int nctas = ((g.nz + FD_TZ - 1) / FD_TZ) * ((g.nx + FD_TX - 1) / FD_TX);
+  double* part = diag ? w.partial : nullptr;
+  int st;
+  if (eq->integrator == MGB_INT_EXPLICIT) {
+    st = fd_stage(p, eq, w, q, q, h, curr, dt, FD_EXPLICIT, part, s, et);
+  } else if (eq->integrator == MGB_INT_PECE) {
+    // predict into w.qpred, then evaluate there and correct q in place; the
+    // corrector's f* goes to the next slot, which the caller's advance makes
+    // the next step's f0 slot.
+    st = fd_stage(p, eq, w, q, q, h, curr, dt, FD_PREDICT, part, s, et);
+    if (st) return st;
+    const int next = (curr + 1) % eq->order;
+    st = fd_stage(p, eq, w, q, w.qpred, h, next, dt, FD_CORRECT, nullptr, s, et);
+  } else {
+    return fail(MGB_ERR_UNSUPPORTED,
+                "semi-implicit integration needs a fully spectral grid (melvin/Integrator.py:78-81)");
+  }
+  if (st) return st;
+  if (diag) return pw_finish_diag(w.partial, nctas, 1.0 / ((double)g.nx * (double)g.nz), diag, s);
+  return MGB_OK;
+}
+
+}  // namespace mgb

@@ -1,0 +1,517 @@
+// Fourier-x / finite-difference-z (Dirichlet) kernels.
+//
+// Layouts (row-major): spectral zd[nn][nz] (x modes n = 0..nn-1 by z
+// points), physical T/double [nx][nz].
+//
+// Transforms are along x only (melvin/SpectralTransformer.py:33-88): the
+// x pass works on tiles of C adjacent z columns; two real z columns are
+// packed into one complex transform of length nx.
+//
+// Timestep (examples/rayleigh_benard_convection.py:97-142):
+//   k_thomas    psi = solve(-w), per-mode Dirichlet tridiagonal
+//               (melvin/LaplacianSolver.py:21-56, 70-79);
+//   k_fd_xinv   ux = -pddz(psi), uz = sddx(psi) and the advected fields to
+//               physical (melvin/utility.py:66-79); writes the diffusion
+//               term kappa * snabla2(q) into the history slot that receives f0;
+//   k_fd_phys   J = pddx(ux q) + pddz(uz q) (melvin/Variable.py:119-128);
+//   k_fd_xfwd   J to spectral, f = -J^ + linear terms + diffusion, explicit
+//               Adams-Bashforth, AB predictor or AM corrector, boundary rules.
+#pragma once
+
+#include "spectral2d_impl.cuh"
+
+namespace mgb {
+
+// Complex columns (pairs of z columns) per CTA of an FDM x pass.
+template <typename T, int N>
+struct FdTile {
+  static constexpr int E = (sizeof(T) == 8) ? 4096 : 8192;
+  static constexpr int P0 = E / N;
+  static constexpr int CP = P0 < 1 ? 1 : (P0 > 32 ? 32 : P0);
+  static constexpr int C = 2 * CP;  // z columns
+};
+
+// pd2dz2 of a complex spectral row at z (interior only), times kappa, plus
+// kappa * d2x n^2 q  ==  kappa * snabla2(q) (melvin/Variable.py:111-113).
+__device__ __forceinline__ zd fd_snabla2(const GridC& g, const zd* row, int n, int z, double kappa) {
+  const int h = g.sdo / 2;
+  const double inv = 1.0 / (g.dz * g.dz);
+  double ax = 0, ay = 0;
+  if (z >= h && z < g.nz - h) {
+    const zd p1 = row[z + 1], c0 = row[z], m1 = row[z - 1];
+    if (g.sdo == 2) {
+      ax = ((p1.x - 2 * c0.x) + m1.x) * inv;
+      ay = ((p1.y - 2 * c0.y) + m1.y) * inv;
+    } else {
+      const zd p2 = row[z + 2], m2 = row[z - 2];
+      ax = ((((-1.0 / 12) * p2.x + (4.0 / 3) * p1.x) - (5.0 / 2) * c0.x) + (4.0 / 3) * m1.x - (1.0 / 12) * m2.x) * inv;
+      ay = ((((-1.0 / 12) * p2.y + (4.0 / 3) * p1.y) - (5.0 / 2) * c0.y) + (4.0 / 3) * m1.y - (1.0 / 12) * m2.y) * inv;
+    }
+  }
+  const zd q = row[z];
+  const double f = g.d2x * (double)(n * n);
+  return mk(kappa * (f * q.x + ax), kappa * (f * q.y + ay));
+}
+
+// ---------------------------------------------------------------------------
+// Thomas solve of the per-mode Dirichlet Poisson systems.  The factors
+// (inverse pivots and modified upper diagonal) are precomputed per plan.
+// One thread solves the real or imaginary part of one mode; rows are staged
+// through shared memory so global accesses stay coalesced.
+// ---------------------------------------------------------------------------
+
+constexpr int TH_MODES = 8;  // modes per CTA
+
+static __global__ void __launch_bounds__(NT) k_thomas(GridC g, const zd* __restrict__ rhs, double rhs_sign,
+                                               zd* __restrict__ out, const double* __restrict__ inv_piv,
+                                               const double* __restrict__ cp) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  zd* rows = reinterpret_cast<zd*>(smem_raw);  // [TH_MODES][nz]
+  const int n0 = blockIdx.x * TH_MODES;
+  const int nz = g.nz;
+  const int nm = min(TH_MODES, g.nn - n0);
+  for (int e = threadIdx.x; e < nm * nz; e += NT) {
+    const zd v = rhs[(size_t)n0 * nz + e];
+    rows[e] = mk(rhs_sign * v.x, rhs_sign * v.y);
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t < 2 * nm) {
+    const int mode = t >> 1, part = t & 1;
+    double* d = reinterpret_cast<double*>(rows + (size_t)mode * nz) + part;  // stride 2 doubles
+    const double* ip = inv_piv + (size_t)(n0 + mode) * nz;
+    const double* c = cp + (size_t)(n0 + mode) * nz;
+    const double a = 1.0 / (g.dz * g.dz);
+    // forward sweep: row 0 and row nz-1 are identity rows
+    double prev = d[0];
+    for (int j = 1; j < nz - 1; ++j) {
+      const double v = (d[2 * j] - a * prev) * ip[j];
+      d[2 * j] = v;
+      prev = v;
+    }
+    // back substitution
+    double next = d[2 * (nz - 1)];
+    for (int j = nz - 2; j >= 1; --j) {
+      const double v = d[2 * j] - c[j] * next;
+      d[2 * j] = v;
+      next = v;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nm * nz; e += NT) out[(size_t)n0 * nz + e] = rows[e];
+}
+
+// ---------------------------------------------------------------------------
+// x pass inverse: spectral rows n < nn of up to 3 fields -> physical.
+// ---------------------------------------------------------------------------
+
+// What an x-inverse job transforms.
+enum FdKind : int {
+  FD_COPY = 0,  // the spectral field itself
+  FD_UX = 1,    // ux = -pddz(psi): the Dirichlet z stencil commutes with the x transform
+  FD_UZ = 2     // uz = sddx(psi) = (2*pi*i/lx) n psi (melvin/utility.py:76-79)
+};
+
+struct FdXinvJob {
+  const zd* src;
+  void* phys;     // T [nx][nz]
+  zd* diff_out;   // optional: kappa * snabla2(src) -> history slot
+  double kappa;
+  int kind;       // FdKind
+  zd* spec_out;   // optional: the transformed spectral field (uz spectral data)
+};
+
+// First-derivative z stencil of a complex spectral row (Dirichlet: the
+// outer sdo/2 points are 0), scaled by inv = 1/(2dz) or 1/(3dz).
+__device__ __forceinline__ zd fd_ddz_row(const zd* row, int z, int nz, int sdo, double inv) {
+  const int h = sdo / 2;
+  if (z < h || z >= nz - h) return mk(0.0, 0.0);
+  const zd p1 = row[z + 1], m1 = row[z - 1];
+  if (sdo == 2) return mk((p1.x - m1.x) * inv, (p1.y - m1.y) * inv);
+  const zd p2 = row[z + 2], m2 = row[z - 2];
+  return mk((((-0.25 * p2.x + 2 * p1.x) - 2 * m1.x) + 0.25 * m2.x) * inv,
+            (((-0.25 * p2.y + 2 * p1.y) - 2 * m1.y) + 0.25 * m2.y) * inv);
+}
+
+struct FdXinvArgs {
+  GridC g;
+  FdXinvJob job[5];
+  double fdz;    // 1/(2dz) or 1/(3dz)
+  const void* tw;
+};
+
+template <typename T, int N>
+__global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
+  constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
+  const GridC& g = a.g;
+  const FdXinvJob jb = a.job[blockIdx.y];
+  const int z0 = blockIdx.x * C;
+  for (int e = threadIdx.x; e < N * CP; e += NT) buf[e] = mk<T>(0, 0);
+  __syncthreads();
+  for (int e = threadIdx.x; e < g.nn * CP; e += NT) {
+    const int n = e / CP, j = e - n * CP;
+    const int za = z0 + 2 * j, zb = za + 1;
+    const zd* row = jb.src + (size_t)n * g.nz;
+    zd A = mk(0.0, 0.0), B = mk(0.0, 0.0);
+    if (jb.kind == FD_UX) {
+      if (za < g.nz) A = fd_ddz_row(row, za, g.nz, g.sdo, a.fdz);
+      if (zb < g.nz) B = fd_ddz_row(row, zb, g.nz, g.sdo, a.fdz);
+      A = mk(-A.x, -A.y);
+      B = mk(-B.x, -B.y);
+    } else {
+      if (za < g.nz) A = row[za];
+      if (zb < g.nz) B = row[zb];
+      if (jb.kind == FD_UZ) {
+        const double b = g.dfx * (double)n;
+        A = mk(-(b * A.y), b * A.x);
+        B = mk(-(b * B.y), b * B.x);
+      }
+    }
+    if (jb.spec_out) {
+      if (za < g.nz) jb.spec_out[(size_t)n * g.nz + za] = A;
+      if (zb < g.nz) jb.spec_out[(size_t)n * g.nz + zb] = B;
+    }
+    put_pair<T, N, CP>(buf, j, n, mk((T)A.x, (T)A.y), mk((T)B.x, (T)B.y));
+    if (jb.diff_out) {
+      if (za < g.nz) jb.diff_out[(size_t)n * g.nz + za] = fd_snabla2(g, row, n, za, jb.kappa);
+      if (zb < g.nz) jb.diff_out[(size_t)n * g.nz + zb] = fd_snabla2(g, row, n, zb, jb.kappa);
+    }
+  }
+  __syncthreads();
+  block_fft<T, N, CP, CP, NT, +1>(buf, (const cx<T>*)a.tw);
+  T* out = (T*)jb.phys;
+  for (int e = threadIdx.x; e < N * CP; e += NT) {
+    const int x = e / CP, j = e - x * CP;
+    const int za = z0 + 2 * j;
+    const cx<T> v = buf[e];
+    if (za < g.nz) out[(size_t)x * g.nz + za] = v.x;
+    if (za + 1 < g.nz) out[(size_t)x * g.nz + za + 1] = v.y;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Physical stencil pass on a 2D tile with a halo of h = sdo/2 points.
+// ---------------------------------------------------------------------------
+
+constexpr int FD_TX = 16, FD_TZ = 64;
+
+struct FdPhysArgs {
+  GridC g;
+  const void* ux;    // T [nx][nz]
+  const void* uz;    // T [nx][nz]
+  const void* q[3];  // T [nx][nz]
+  void* jout[3];     // T [nx][nz]
+  double* partial;   // optional per-CTA diagnostics (sum ux^2+uz^2, max ux, max uz)
+  int nf;
+  double fdx, fdz;   // 1/(2dx) or 1/(3dx); same for z
+};
+
+template <typename T>
+__device__ __forceinline__ T st1(T p2, T p1, T m1, T m2, int sdo, T inv) {
+  if (sdo == 2) return (p1 - m1) * inv;
+  return (((p2 * (T)-0.25 + p1 * (T)2) - m1 * (T)2) + m2 * (T)0.25) * inv;
+}
+
+// J_f = pddx(ux q_f) + pddz(uz q_f) on a 2D tile (x periodic, z Dirichlet:
+// the outer sdo/2 points of pddz stay 0) (melvin/Variable.py:125-127).
+template <typename T>
+__global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
+  constexpr int H = 2;  // storage halo (covers order 4)
+  constexpr int SX = FD_TX + 2 * H, SZ = FD_TZ + 2 * H;
+  __shared__ T s_ux[SX][FD_TZ];  // x halo
+  __shared__ T s_uz[FD_TX][SZ];  // z halo
+  __shared__ T s_q[SX][SZ];
+  const GridC& g = a.g;
+  const int nx = g.nx, nz = g.nz, sdo = g.sdo, h = sdo / 2;
+  const int x0 = blockIdx.y * FD_TX, z0 = blockIdx.x * FD_TZ;
+  const T fdx = (T)a.fdx, fdz = (T)a.fdz;
+  const T* ux = (const T*)a.ux;
+  const T* uz = (const T*)a.uz;
+  for (int e = threadIdx.x; e < SX * FD_TZ; e += NT) {
+    const int i = e / FD_TZ, k = e - i * FD_TZ;
+    const int x = (x0 + i - H + nx) % nx, z = z0 + k;
+    s_ux[i][k] = z < nz ? ux[(size_t)x * nz + z] : (T)0;
+  }
+  for (int e = threadIdx.x; e < FD_TX * SZ; e += NT) {
+    const int i = e / SZ, k = e - i * SZ;
+    const int x = x0 + i, z = z0 + k - H;
+    s_uz[i][k] = (x < nx && z >= 0 && z < nz) ? uz[(size_t)x * nz + z] : (T)0;
+  }
+  __syncthreads();
+  double ke = 0, mx = -INFINITY, mz = -INFINITY;
+  if (a.partial) {
+    for (int e = threadIdx.x; e < FD_TX * FD_TZ; e += NT) {
+      const int i = e / FD_TZ, k = e - i * FD_TZ;
+      if (x0 + i < nx && z0 + k < nz) {
+        const double u = (double)s_ux[i + H][k], w = (double)s_uz[i][k + H];
+        ke += w * w + u * u;
+        mx = (u != u || u > mx) ? u : mx;
+        mz = (w != w || w > mz) ? w : mz;
+      }
+    }
+  }
+  for (int f = 0; f < a.nf; ++f) {
+    const T* q = (const T*)a.q[f];
+    for (int e = threadIdx.x; e < SX * SZ; e += NT) {
+      const int i = e / SZ, k = e - i * SZ;
+      const int x = (x0 + i - H + nx) % nx, z = z0 + k - H;
+      s_q[i][k] = (z >= 0 && z < nz) ? q[(size_t)x * nz + z] : (T)0;
+    }
+    __syncthreads();
+    T* jo = (T*)a.jout[f];
+    for (int e = threadIdx.x; e < FD_TX * FD_TZ; e += NT) {
+      const int i = e / FD_TZ, k = e - i * FD_TZ;
+      const int x = x0 + i, z = z0 + k;
+      if (x >= nx || z >= nz) continue;
+      const int ii = i + H, kk = k + H;
+      const T jx = st1(s_ux[ii + 2][k] * s_q[ii + 2][kk], s_ux[ii + 1][k] * s_q[ii + 1][kk],
+                       s_ux[ii - 1][k] * s_q[ii - 1][kk], s_ux[ii - 2][k] * s_q[ii - 2][kk], sdo, fdx);
+      T jz = 0;
+      if (z >= h && z < nz - h)
+        jz = st1(s_uz[i][kk + 2] * s_q[ii][kk + 2], s_uz[i][kk + 1] * s_q[ii][kk + 1],
+                 s_uz[i][kk - 1] * s_q[ii][kk - 1], s_uz[i][kk - 2] * s_q[ii][kk - 2], sdo, fdz);
+      jo[(size_t)x * nz + z] = jx + jz;
+    }
+    __syncthreads();
+  }
+  if (a.partial) {
+    __shared__ double red[3][NT / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+      ke += __shfl_xor_sync(0xffffffffu, ke, o);
+      const double t1 = __shfl_xor_sync(0xffffffffu, mx, o), t2 = __shfl_xor_sync(0xffffffffu, mz, o);
+      mx = (t1 != t1 || t1 > mx) ? t1 : mx;
+      mz = (t2 != t2 || t2 > mz) ? t2 : mz;
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red[0][threadIdx.x >> 5] = ke;
+      red[1][threadIdx.x >> 5] = mx;
+      red[2][threadIdx.x >> 5] = mz;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double S = 0, MX = -INFINITY, MZ = -INFINITY;
+      for (int i = 0; i < NT / 32; ++i) {
+        S += red[0][i];
+        MX = (red[1][i] != red[1][i] || red[1][i] > MX) ? red[1][i] : MX;
+        MZ = (red[2][i] != red[2][i] || red[2][i] > MZ) ? red[2][i] : MZ;
+      }
+      const int cta = blockIdx.y * gridDim.x + blockIdx.x;
+      a.partial[3 * cta + 0] = S;
+      a.partial[3 * cta + 1] = MX;
+      a.partial[3 * cta + 2] = MZ;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// x pass forward: physical J_f -> spectral, then the update.
+// ---------------------------------------------------------------------------
+
+enum FdMode : int {
+  FD_OUT = 0,       // plain to_spectral into `out` (per-verb API)
+  FD_EXPLICIT = 1,  // q += AB(hist)
+  FD_PREDICT = 2,   // qpred = q + AB(hist)
+  FD_CORRECT = 3    // q = q + AM(hist)
+};
+
+struct FdXfField {
+  int nterms;
+  int tsrc[4];
+  int top[4];
+  double tcoef[4];
+  int bc;
+};
+
+struct FdXfArgs {
+  GridC g;
+  const void* jin[3];  // T [nx][nz]
+  zd* q[3];            // states: read (all modes); written for EXPLICIT / CORRECT
+  const zd* qsrc[3];   // states the linear terms read (q, or the predicted state)
+  zd* qpred[3];        // PREDICT output
+  zd* hist[3];
+  const zd* psi;       // spectral psi of the evaluated state (for src = -1 terms)
+  zd* out;             // FD_OUT target
+  int nf, mode, order, curr;
+  double dt, inv_nx;
+  FdXfField eq[3];
+  const void* tw;
+};
+
+__device__ __forceinline__ zd fd_ab(const zd* h, size_t slot, int order, int curr, zd f0, double dt) {
+  if (order == 2) {
+    const zd f1 = h[(size_t)((curr + 1) & 1) * slot];
+    const double c = dt / 2;
+    return mk(c * (3 * f0.x - f1.x), c * (3 * f0.y - f1.y));
+  }
+  const zd f1 = h[(size_t)((curr + 3) & 3) * slot];
+  const zd f2 = h[(size_t)((curr + 2) & 3) * slot];
+  const zd f3 = h[(size_t)((curr + 1) & 3) * slot];
+  const double c = dt / 24;
+  return mk(c * (((55 * f0.x - 59 * f1.x) + 37 * f2.x) - 9 * f3.x),
+            c * (((55 * f0.y - 59 * f1.y) + 37 * f2.y) - 9 * f3.y));
+}
+
+__device__ __forceinline__ zd fd_am(const zd* h, size_t slot, int order, int curr, zd f0, double dt) {
+  if (order == 2) {
+    const zd f1 = h[(size_t)((curr + 1) & 1) * slot];
+    const double c = dt / 2;
+    return mk(c * (f0.x + f1.x), c * (f0.y + f1.y));
+  }
+  const zd f1 = h[(size_t)((curr + 3) & 3) * slot];
+  const zd f2 = h[(size_t)((curr + 2) & 3) * slot];
+  const zd f3 = h[(size_t)((curr + 1) & 3) * slot];
+  const double c = dt / 24;
+  return mk(c * (((9 * f0.x + 19 * f1.x) - 5 * f2.x) + f3.x), c * (((9 * f0.y + 19 * f1.y) - 5 * f2.y) + f3.y));
+}
+
+// Boundary rules of examples/rayleigh_benard_convection.py:112-142 for
+// point (n, z); `e` = 1 (order 2) or 2 (order 4) edge points.
+__device__ __forceinline__ zd fd_bc(zd v, int bc, int n, int z, int nz, int e) {
+  const bool lower = z < e, upper = z >= nz - e;
+  if (bc & MGB_BC_DIRICHLET_W) {
+    if (n == 0 || lower || upper) return mk(0.0, 0.0);
+  }
+  if (bc & MGB_BC_DIRICHLET_T) {
+    if (n == 0) {
+      if (lower) return mk(1.0, 0.0);
+      if (upper) return mk(0.0, 0.0);
+    } else if (lower || upper) {
+      return mk(0.0, 0.0);
+    }
+  }
+  return v;
+}
+
+template <typename T, int N, int F>
+__global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
+  constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
+  const GridC& g = a.g;
+  const int z0 = blockIdx.x * C;
+#pragma unroll
+  for (int f = 0; f < F; ++f) {
+    const T* J = (const T*)a.jin[f];
+    cx<T>* bf = buf + f * N * CP;
+    for (int e = threadIdx.x; e < N * CP; e += NT) {
+      const int x = e / CP, j = e - x * CP;
+      const int za = z0 + 2 * j;
+      const T va = za < g.nz ? J[(size_t)x * g.nz + za] : (T)0;
+      const T vb = za + 1 < g.nz ? J[(size_t)x * g.nz + za + 1] : (T)0;
+      bf[e] = mk(va, vb);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int f = 0; f < F; ++f) block_fft<T, N, CP, CP, NT, -1>(buf + f * N * CP, (const cx<T>*)a.tw);
+  const size_t slot = (size_t)g.nn * g.nz;
+  const int e_bc = g.sdo / 2;
+  for (int e = threadIdx.x; e < g.nn * C; e += NT) {
+    const int n = e / C, c = e - n * C, z = z0 + c;
+    if (z >= g.nz) continue;
+    const size_t idx = (size_t)n * g.nz + z;
+    const int j = c >> 1, part = c & 1;
+    if (a.mode == FD_OUT) {
+      cx<T> A, B;
+      get_pair<T, N, CP>(buf, j, n, A, B);
+      const cx<T> v = part ? B : A;
+      a.out[idx] = mk((double)v.x * a.inv_nx, (double)v.y * a.inv_nx);
+      continue;
+    }
+    zd qs[F];
+#pragma unroll
+    for (int f = 0; f < F; ++f) qs[f] = a.qsrc[f][idx];
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      cx<T> A, B;
+      get_pair<T, N, CP>(buf + f * N * CP, j, n, A, B);
+      const cx<T> v = part ? B : A;
+      // f = -vec_dot_nabla + linear terms + diffusion (already in the slot)
+      zd* hs = a.hist[f] + (size_t)a.curr * slot + idx;
+      const zd d = *hs;
+      zd fv = mk(d.x - (double)v.x * a.inv_nx, d.y - (double)v.y * a.inv_nx);
+      const FdXfField& eq = a.eq[f];
+      for (int t = 0; t < eq.nterms; ++t) {
+        const int sidx = eq.tsrc[t];
+        zd s = sidx < 0 ? a.psi[idx] : qs[0];
+#pragma unroll
+        for (int q2 = 1; q2 < F; ++q2)
+          if (sidx == q2) s = qs[q2];
+        if (eq.top[t] == 1) {
+          const double b = g.dfx * (double)n;
+          s = mk(-(b * s.y), b * s.x);
+        }
+        fv = mk(fv.x + eq.tcoef[t] * s.x, fv.y + eq.tcoef[t] * s.y);
+      }
+      *hs = fv;
+      const zd q0 = a.q[f][idx];
+      zd qn;
+      if (a.mode == FD_CORRECT) {
+        const zd am = fd_am(a.hist[f] + idx, slot, a.order, a.curr, fv, a.dt);
+        qn = mk(q0.x + am.x, q0.y + am.y);
+      } else {
+        const zd ab = fd_ab(a.hist[f] + idx, slot, a.order, a.curr, fv, a.dt);
+        qn = mk(q0.x + ab.x, q0.y + ab.y);
+      }
+      qn = fd_bc(qn, eq.bc, n, z, g.nz, e_bc);
+      if (a.mode == FD_PREDICT)
+        a.qpred[f][idx] = qn;
+      else
+        a.q[f][idx] = qn;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+
+template <typename T, int N>
+cudaError_t launch_fd_xinv(const FdXinvArgs& a, int njobs, cudaStream_t s) {
+  constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
+  const size_t smem = (size_t)N * CP * sizeof(cx<T>);
+  cudaError_t e = prep_smem(k_fd_xinv<T, N>, smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid((a.g.nz + C - 1) / C, njobs);
+  k_fd_xinv<T, N><<<grid, NT, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T, int N, int F>
+cudaError_t launch_fd_xfwd(const FdXfArgs& a, cudaStream_t s) {
+  constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
+  constexpr size_t smem = (size_t)F * N * CP * sizeof(cx<T>);
+  if constexpr (smem > kMaxDynSmem) {
+    return cudaErrorInvalidConfiguration;
+  } else {
+    cudaError_t e = prep_smem(k_fd_xfwd<T, N, F>, smem);
+    if (e != cudaSuccess) return e;
+    k_fd_xfwd<T, N, F><<<(a.g.nz + C - 1) / C, NT, smem, s>>>(a);
+    return cudaGetLastError();
+  }
+}
+
+struct FdLaunchers {
+  cudaError_t (*xinv[2])(const FdXinvArgs&, int, cudaStream_t);  // [split]
+  cudaError_t (*xfwd[2][3])(const FdXfArgs&, cudaStream_t);      // [split][F-1]
+};
+
+template <int N>
+FdLaunchers make_fd_launchers() {
+  FdLaunchers L;
+  L.xinv[0] = launch_fd_xinv<double, N>;
+  L.xinv[1] = launch_fd_xinv<float, N>;
+  L.xfwd[0][0] = launch_fd_xfwd<double, N, 1>;
+  L.xfwd[0][1] = launch_fd_xfwd<double, N, 2>;
+  L.xfwd[0][2] = launch_fd_xfwd<double, N, 3>;
+  L.xfwd[1][0] = launch_fd_xfwd<float, N, 1>;
+  L.xfwd[1][1] = launch_fd_xfwd<float, N, 2>;
+  L.xfwd[1][2] = launch_fd_xfwd<float, N, 3>;
+  return L;
+}
+
+const FdLaunchers* fd_launchers(int N);
+
+}  // namespace mgb

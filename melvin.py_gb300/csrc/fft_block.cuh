@@ -1,0 +1,144 @@
+// Block-level Stockham FFT held in shared memory.
+//
+// A CTA transforms C interleaved columns of length N (a power of two) that
+// sit in shared memory as buf[x * CS + c] (x = position along the transform,
+// c = column, CS >= C the interleave stride).  Each pass is a radix-8, -4 or
+// -2 butterfly computed in registers: a thread reads all R inputs of its
+// butterflies, the CTA synchronises, and the thread writes the R outputs to
+// the Stockham (self-sorting) positions, so the result ends in natural order
+// without a bit-reversal pass.  Consecutive threads take consecutive columns
+// of the same butterfly, so the reads of every pass are contiguous in shared
+// memory.
+//
+// Twiddles come from a device table tw[t] = exp(-2*pi*i*t/N), t in [0, N),
+// computed on the host in long double; the inverse direction uses their
+// conjugates.  DIR = -1 is the forward transform exp(-...), DIR = +1 the
+// unnormalised inverse exp(+...).
+#pragma once
+
+#include "common.cuh"
+
+namespace mgb {
+
+template <int R, int DIR, typename T>
+__device__ __forceinline__ void dft4(cx<T>& a0, cx<T>& a1, cx<T>& a2, cx<T>& a3) {
+  cx<T> t0 = a0 + a2, t1 = a0 - a2, t2 = a1 + a3, t3 = mul_i<DIR>(a1 - a3);
+  a0 = t0 + t2;
+  a2 = t0 - t2;
+  a1 = t1 + t3;
+  a3 = t1 - t3;
+}
+
+template <int R, int DIR, typename T>
+struct Dft;
+
+template <int DIR, typename T>
+struct Dft<2, DIR, T> {
+  static __device__ __forceinline__ void run(cx<T>* a) {
+    cx<T> t = a[0] - a[1];
+    a[0] = a[0] + a[1];
+    a[1] = t;
+  }
+};
+
+template <int DIR, typename T>
+struct Dft<4, DIR, T> {
+  static __device__ __forceinline__ void run(cx<T>* a) { dft4<4, DIR>(a[0], a[1], a[2], a[3]); }
+};
+
+template <int DIR, typename T>
+struct Dft<8, DIR, T> {
+  // Radix-8 as two radix-4 halves (even / odd inputs) joined by the
+  // eighth-roots of unity w^k, w = exp(DIR * 2*pi*i/8).
+  static __device__ __forceinline__ void run(cx<T>* a) {
+    const T s = (T)0.70710678118654752440084436210484903928;
+    cx<T> e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6];
+    cx<T> o0 = a[1], o1 = a[3], o2 = a[5], o3 = a[7];
+    dft4<4, DIR>(e0, e1, e2, e3);
+    dft4<4, DIR>(o0, o1, o2, o3);
+    // o1 *= s (1 + DIR i); o2 *= DIR i; o3 *= s (-1 + DIR i)
+    o1 = mk((o1.x - (T)DIR * o1.y) * s, (o1.y + (T)DIR * o1.x) * s);
+    o2 = mul_i<DIR>(o2);
+    o3 = mk((-o3.x - (T)DIR * o3.y) * s, (-o3.y + (T)DIR * o3.x) * s);
+    a[0] = e0 + o0;
+    a[4] = e0 - o0;
+    a[1] = e1 + o1;
+    a[5] = e1 - o1;
+    a[2] = e2 + o2;
+    a[6] = e2 - o2;
+    a[3] = e3 + o3;
+    a[7] = e3 - o3;
+  }
+};
+
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+
+// Radix of the pass that starts with sub-transform length NS.
+template <int N, int NS>
+struct PassRadix {
+  static constexpr int rem = N / NS;
+  static constexpr int value = (rem >= 8 && rem != 16) ? 8 : (rem >= 4 ? 4 : 2);
+};
+
+template <typename T, int N, int C, int CS, int NT, int DIR, int R, int NS>
+__device__ __forceinline__ void stockham_pass(cx<T>* buf, const cx<T>* __restrict__ tw) {
+  constexpr int NB = C * (N / R);
+  constexpr int BPT = (NB + NT - 1) / NT;
+  constexpr int TWS = N / (R * NS);
+  cx<T> v[BPT][R];
+#pragma unroll
+  for (int t = 0; t < BPT; ++t) {
+    const int b = threadIdx.x + t * NT;
+    if (NB % NT == 0 || b < NB) {
+      const int c = b % C, i = b / C;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[t][r] = buf[(i + r * (N / R)) * CS + c];
+      if (NS > 1) {
+        const int k = i & (NS - 1);
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          const cx<T> w = tw[r * k * TWS];
+          v[t][r] = DIR < 0 ? cmul(v[t][r], w) : cmulc(v[t][r], w);
+        }
+      }
+      Dft<R, DIR, T>::run(v[t]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < BPT; ++t) {
+    const int b = threadIdx.x + t * NT;
+    if (NB % NT == 0 || b < NB) {
+      const int c = b % C, i = b / C;
+      const int k = i & (NS - 1);
+      const int base = (i - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) buf[(base + r * NS) * CS + c] = v[t][r];
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int N, int C, int CS, int NT, int DIR, int NS, bool DONE = (NS >= N)>
+struct FftPasses {
+  static __device__ __forceinline__ void run(cx<T>* buf, const cx<T>* __restrict__ tw) {
+    constexpr int R = PassRadix<N, NS>::value;
+    stockham_pass<T, N, C, CS, NT, DIR, R, NS>(buf, tw);
+    FftPasses<T, N, C, CS, NT, DIR, NS * R>::run(buf, tw);
+  }
+};
+
+template <typename T, int N, int C, int CS, int NT, int DIR, int NS>
+struct FftPasses<T, N, C, CS, NT, DIR, NS, true> {
+  static __device__ __forceinline__ void run(cx<T>*, const cx<T>* __restrict__) {}
+};
+
+// Transform columns [0, C) of buf (stride CS) in place; the caller must have
+// synchronised after filling buf.  Ends with a __syncthreads().
+template <typename T, int N, int C, int CS, int NT, int DIR>
+__device__ __forceinline__ void block_fft(cx<T>* buf, const cx<T>* __restrict__ tw) {
+  static_assert((N & (N - 1)) == 0 && N >= 4, "power-of-two length");
+  FftPasses<T, N, C, CS, NT, DIR, 1>::run(buf, tw);
+}
+
+}  // namespace mgb

@@ -1,0 +1,97 @@
+// Host-side plan object and internal launchers shared by the .cu files.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+struct mgb_plan {
+  mgb_grid grid;
+  mgb::GridC g;
+  // Twiddle tables exp(-2*pi*i*t/N), t in [0, N): x axis and (fully
+  // spectral) z axis, in double and float.
+  void* tw_x_d = nullptr;
+  void* tw_x_f = nullptr;
+  void* tw_z_d = nullptr;
+  void* tw_z_f = nullptr;
+  // FDM-z: Thomas factors of the per-mode Dirichlet Poisson matrices,
+  // [nn][nz] each (inverse pivots and modified upper diagonals).
+  double* th_inv = nullptr;
+  double* th_cp = nullptr;
+  int device = 0;
+};
+
+namespace mgb {
+
+constexpr int NT = 256;  // threads per CTA for every transform kernel
+
+// Record a one-line error for mgb_last_error and return `status`.
+int fail(int status, const char* fmt, ...);
+int cuda_check(cudaError_t e, const char* what);
+#define MGB_CUDA(call)                                       \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return ::mgb::cuda_check(e_, #call); \
+  } while (0)
+#define MGB_LAUNCH_CHECK() MGB_CUDA(cudaGetLastError())
+
+// Bytes of one transform intermediate (nx rows x ld cols) of complex T.
+inline size_t inter_bytes(const GridC& g, bool split) {
+  return (size_t)g.nx * (size_t)g.cols * (split ? 8 : 16);
+}
+
+// ---- fully spectral family (spectral2d.cu) ----
+int fs_to_physical(const mgb_plan* p, const zd* spec, double* phys, void* work, cudaStream_t s);
+int fs_to_spectral(const mgb_plan* p, const double* phys, zd* spec, void* work, cudaStream_t s);
+int fs_vec_dot_nabla(const mgb_plan* p, const zd* q, double* q_phys, const double* ux,
+                     const double* uz, zd* out, void* work, cudaStream_t s);
+int fs_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* ux_s, zd* uz_s, double* ux,
+                double* uz, void* work, cudaStream_t s);
+// Optional per-kernel timing: ev[0] is recorded before the first kernel and
+// ev[k] after kernel k, for k < nev.
+struct EventTrack {
+  cudaEvent_t* ev = nullptr;
+  int nev = 0;
+  int k = 0;
+  void mark(cudaStream_t s) {
+    if (ev && k < nev) cudaEventRecord(ev[k], s);
+    ++k;
+  }
+};
+
+int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist,
+            int curr, double dt, void* work, double* diag, cudaStream_t s, EventTrack* et = nullptr);
+size_t fs_step_workspace(const mgb_plan* p, int nfields);
+
+// ---- Fourier-x / Dirichlet-z family (fdm.cu) ----
+int fd_to_physical(const mgb_plan* p, const zd* spec, double* phys, cudaStream_t s);
+int fd_to_spectral(const mgb_plan* p, const double* phys, zd* spec, cudaStream_t s);
+int fd_poisson(const mgb_plan* p, const zd* rhs, zd* out, cudaStream_t s);
+int fd_vec_dot_nabla(const mgb_plan* p, const zd* q, double* q_phys, const double* ux,
+                     const double* uz, zd* out, void* work, cudaStream_t s);
+int fd_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* uz_s, double* psi_phys, double* ux,
+                double* uz, void* work, cudaStream_t s);
+int fd_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist,
+            int curr, double dt, void* work, double* diag, cudaStream_t s, EventTrack* et = nullptr);
+size_t fd_step_workspace(const mgb_plan* p, int nfields);
+size_t fd_verb_workspace(const mgb_plan* p);
+int fd_plan_init(mgb_plan* p);
+
+// ---- pointwise family (pointwise.cu) ----
+int pw_pddx(const mgb_plan* p, const double* in, double* out, cudaStream_t s);
+int pw_pddz(const mgb_plan* p, const double* in, double* out, cudaStream_t s);
+int pw_spectral_derivative(const mgb_plan* p, int kind, const zd* in, zd* out, cudaStream_t s);
+int pw_laplacian(const mgb_plan* p, double* lap, cudaStream_t s);
+int pw_poisson_spectral(const mgb_plan* p, const zd* rhs, zd* out, cudaStream_t s);
+int pw_integrate_semi_implicit(const mgb_plan* p, zd* var, zd* hist, int order, int curr,
+                               double dt, double alpha, const double* lin_op, cudaStream_t s);
+int pw_integrate_explicit(const mgb_plan* p, zd* var, zd* hist, int order, int curr, double dt,
+                          const zd* diffusion, cudaStream_t s);
+int pw_adams(const mgb_plan* p, int corrector, const zd* hist, int order, int curr, double dt,
+             zd* out, cudaStream_t s);
+int pw_diagnostics(const mgb_plan* p, const double* ux, const double* uz, double* out, void* work,
+                   cudaStream_t s);
+// Fold per-CTA partials [n][3] (sum, max, max) into out[3] = {0.5*sum/(nx*nz), max, max}.
+int pw_finish_diag(const double* partial, int n, double inv_npts, double* out, cudaStream_t s);
+
+}  // namespace mgb

@@ -1,0 +1,129 @@
+"""Parity of every per-verb GPU kernel with the reference outputs (golden
+vectors) and with the oracle at larger sizes.  FP64 throughout: the
+tolerance is 1e-12 relative L2 (differences come only from the FFT
+algorithm and the order of floating-point operations)."""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from cases import VERB_CASES, grid_of, params_dict
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def make_sim(g, integrator, order, precision="double"):
+    import melvin
+
+    p = melvin.Parameters(params_dict(g, integrator, order, precision=precision))
+    return melvin.Simulation(p, torch), p
+
+
+def basis(g):
+    from melvin import BasisFunctions as B
+
+    return [B.COMPLEX_EXP, B.FDM if g.fdm_z else B.COMPLEX_EXP]
+
+
+def host(t):
+    return t.detach().cpu().numpy() if isinstance(t, torch.Tensor) else np.asarray(t)
+
+
+@pytest.mark.parametrize("tag", list(VERB_CASES))
+def test_verbs_match_reference(cuda, golden, tag):
+    from melvin.utility import calc_kinetic_energy, calc_velocity_from_vorticity
+
+    nx, nz, lx, lz, fdm, order, iorder, integ = VERB_CASES[tag]
+    g = grid_of(tag)
+    sim, p = make_sim(g, integ, iorder)
+    bf = basis(g)
+    st, sd = sim._spectral_trans, sim._spatial_diff
+    s, ph, ux, uz = (golden[f"{tag}/in_{k}"] for k in ("spec", "phys", "ux", "uz"))
+    got = {
+        "to_physical": st.to_physical(s, basis_functions=bf),
+        "to_spectral": st.to_spectral(ph, basis_functions=bf),
+        "pddx": sd.pddx(ph),
+        "pddz": sd.pddz(ph),
+    }
+    q = sim.make_variable("q", bf)
+    q.sets(s)
+    got["sddx"] = q.sddx()
+    got["sd2dx2"] = q.sd2dx2()
+    got["snabla2"] = q.snabla2()
+    got["lap"] = q.lap()
+    if fdm:
+        got["pd2dz2"] = sd.pd2dz2(s)
+    else:
+        got["sddz"] = q.sddz()
+        got["sd2dz2"] = q.sd2dz2()
+    got["vec_dot_nabla"] = q.vec_dot_nabla(torch.as_tensor(ux, device=cuda), torch.as_tensor(uz, device=cuda))
+    got["vec_dot_nabla_phys"] = q.getp()
+    sim.init_laplacian_solver(bf)
+    solver = sim.get_laplacian_solver()
+    got["poisson"] = solver.solve(s)
+    w, psi, vx, vz = (sim.make_variable(n, bf) for n in ("w", "psi", "ux", "uz"))
+    w.sets(s)
+    calc_velocity_from_vorticity(w, psi, vx, vz, solver)
+    got["vel_psi"], got["vel_ux_p"], got["vel_uz_p"] = psi.gets(), vx.getp(), vz.getp()
+    if fdm:
+        got["vel_psi_p"] = psi.getp()
+    else:
+        got["vel_ux_s"], got["vel_uz_s"] = vx.gets(), vz.gets()
+    got["ke"] = calc_kinetic_energy(vx, vz, torch, p)
+    dv = sim.make_derivative("dq")
+    dv._data.copy_(torch.as_tensor(golden[f"{tag}/hist"], device=cuda))
+    dv.set_curr_idx(1)
+    got["ab"] = sim._integrator.predictor(dv)
+    got["am"] = sim._integrator.corrector(dv)
+    torch.cuda.synchronize()
+    bad = {k: rel_l2(host(v), golden[f"{tag}/{k}"]) for k, v in got.items()}
+    assert all(e < TOL for e in bad.values()), {k: f"{e:.2e}" for k, e in bad.items() if e >= TOL}
+
+
+@pytest.mark.parametrize(
+    "nx,nz,fdm,order",
+    [(256, 256, False, 2), (128, 512, False, 4), (2048, 64, False, 2), (128, 65, True, 4), (1024, 33, True, 2),
+     (16, 16, False, 2), (4096, 16, False, 4)],
+)
+def test_transforms_and_jacobian_vs_oracle(cuda, nx, nz, fdm, order):
+    """Random inputs at sizes beyond the golden set, including the smallest
+    and largest transform lengths built."""
+    g = O.Grid(nx, nz, 2.0, 1.5, fdm, order)
+    sim, p = make_sim(g, "explicit" if fdm else "semi-implicit", 2)
+    bf = basis(g)
+    rng = np.random.default_rng(nx + nz)
+    s = rng.standard_normal(g.spectral_shape) + 1j * rng.standard_normal(g.spectral_shape)
+    ph, ux, uz = (rng.standard_normal((nx, nz)) for _ in range(3))
+    st = sim._spectral_trans
+    assert rel_l2(host(st.to_physical(s, basis_functions=bf)), O.to_physical(g, s)) < TOL
+    assert rel_l2(host(st.to_spectral(ph, basis_functions=bf)), O.to_spectral(g, ph)) < TOL
+    q = sim.make_variable("q", bf)
+    q.sets(s)
+    v = q.vec_dot_nabla(torch.as_tensor(ux, device=cuda), torch.as_tensor(uz, device=cuda))
+    want, want_p = O.vec_dot_nabla(g, s, ux, uz)
+    assert rel_l2(host(v), want) < TOL
+    assert rel_l2(host(q.getp()), want_p) < TOL
+
+
+def test_round_trip_property_2048(cuda):
+    """to_spectral(to_physical(s)) == s for a dealiased spectrum, at 2048^2
+    (size-independent property)."""
+    g = O.Grid(2048, 2048, 2 * np.pi, 2 * np.pi)
+    sim, p = make_sim(g, "semi-implicit", 2)
+    rng = np.random.default_rng(1)
+    s = torch.as_tensor(O.to_spectral(g, rng.standard_normal((2048, 2048))), device=cuda)
+    st = sim._spectral_trans
+    back = st.to_spectral(st.to_physical(s))
+    assert rel_l2(host(back), host(s)) < TOL
+
+
+def test_unsupported_sizes_fail_loudly(cuda):
+    import melvin
+    from melvin._native import MelvinUnsupported
+
+    p = melvin.Parameters({"nx": 96, "nz": 64, "lx": 1.0, "lz": 1.0, "final_time": 1.0})
+    with pytest.raises(MelvinUnsupported):
+        melvin.Simulation(p, torch)
