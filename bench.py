@@ -300,6 +300,30 @@ def run_reference(args):
     return 0
 
 
+def run_only(args):
+    """Warm-up plus timed fused steps of one precision and nothing else (the
+    command profiled with ncu)."""
+    import torch
+
+    from melvin import workloads
+
+    _, _, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    n = args.n
+    w0 = workloads.decaying_turbulence(n, n, seed=0)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
+    sim, w, dw, step = make_run(n, "split" if args.only == "split" else "double", device, w0)
+    for _ in range(args.warmup):
+        step.step()
+    torch.cuda.synchronize()
+    per_step, per_kernel = timed_steps(step, args.steps, flush)
+    print(json.dumps({"only": args.only, "n": n, "steps": args.steps,
+                      "ms_per_step": round(statistics.mean(per_step), 4),
+                      "kernel_ms": [round(statistics.mean(k), 4) for k in per_kernel]}), flush=True)
+    return 0
+
+
 def run_native(args):
     import numpy as np
     import torch
@@ -416,7 +440,7 @@ def run_native(args):
                       "ms_per_step": round(secs_s / args.steps * 1e3, 4),
                       "speedup_vs_fp64": round(value_s / value, 3), "roofline": roof_s, **acc},
             "cpu_baseline": cpu,
-            "gpu_launches": step.kernel_count() * args.steps * 2,
+            "gpu_launches": step.kernel_count() * args.steps,
             "clocks": clocks.summary(),
             "wall_s_fp64_timed": round(wall, 3),
         }
@@ -435,11 +459,14 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
     ap.add_argument("--n", type=int, default=2048, help="grid points per side (default 2048)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--only", choices=["fp64", "split"], help="run only the timed fused steps of one precision")
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "native":
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.only:
+        return run_only(args)
     return run_native(args)
 
 

@@ -201,6 +201,15 @@ typedef struct mgb_equation {
   mgb_field_eq f[3];
 } mgb_equation;
 
+/* Compute into `work` the per-mode update coefficients of `eq` at `dt`
+ * (for the fully spectral semi-implicit update: (1 + (1-alpha) dt L) /
+ * (1 - alpha dt L) and the Adams-Bashforth weight over (1 - alpha dt L),
+ * L = kappa * lap; melvin/Integrator.py:58-63).  Call it before mgb_step
+ * and again whenever eq, dt or the workspace change; mgb_step returns
+ * MGB_ERR_INVALID when the last preparation on the plan does not match.
+ * A no-op for FDM-z plans. */
+int mgb_step_prepare(const mgb_plan* plan, const mgb_equation* eq, double dt, void* work, void* stream);
+
 /* One timestep of the whole loop body (velocity from vorticity, nonlinear
  * terms, linear terms, update, boundary rules) for `eq`, fused into a few
  * kernels.  q[f]: spectral states (updated in place); hist[f]: histories;

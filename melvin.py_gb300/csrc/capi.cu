@@ -73,6 +73,8 @@ static void release(mgb_plan* p) {
   cudaFree(p->tw_z_f);
   cudaFree(p->th_inv);
   cudaFree(p->th_cp);
+  cudaFree(p->tab_d);
+  cudaFree(p->tab_f);
   delete p;
 }
 
@@ -140,6 +142,7 @@ int mgb_plan_create(const mgb_grid* grid, mgb_plan** out) {
   cudaGetDevice(&p->device);
   int st = upload_twiddles(G.nx, &p->tw_x_d, &p->tw_x_f);
   if (!st && !G.fdm_z) st = upload_twiddles(G.nz, &p->tw_z_d, &p->tw_z_f);
+  if (!st && !G.fdm_z) st = fs_plan_init(p);
   if (!st && G.fdm_z) st = fd_plan_init(p);
   if (st) {
     release(p);
@@ -337,6 +340,28 @@ static int step_impl(const mgb_plan* p, const mgb_equation* eq, void* const* q, 
 int mgb_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist, int32_t curr, double dt,
              void* work, double* diag, void* stream) {
   return step_impl(p, eq, q, hist, curr, dt, work, diag, stream, nullptr);
+}
+
+int mgb_step_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void* work, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(eq);
+  CHECK_PTR(work);
+  const int F = eq->nfields;
+  if (F < 1 || F > 3) return fail(MGB_ERR_INVALID, "nfields=%d (1..3)", F);
+  if (eq->order != 2 && eq->order != 4) return fail(MGB_ERR_INVALID, "integrator_order=%d (2 or 4)", eq->order);
+  if (p->g.fdm) return MGB_OK;  // the Dirichlet update needs no per-mode coefficients
+  int st = fs_prepare(p, eq, dt, work, (cudaStream_t)stream);
+  std::lock_guard<std::mutex> lock(p->mu);
+  PrepRecord& pr = p->prep;
+  pr.valid = st == MGB_OK;
+  pr.work = work;
+  pr.dt = dt;
+  pr.alpha = eq->alpha;
+  pr.nfields = F;
+  pr.integrator = eq->integrator;
+  pr.order = eq->order;
+  for (int f = 0; f < 3; ++f) pr.kappa[f] = f < F ? eq->f[f].kappa : 0.0;
+  return st;
 }
 
 int mgb_step_kernel_count(const mgb_plan* p, const mgb_equation* eq, int32_t* count) {

@@ -3,7 +3,20 @@
 
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "common.cuh"
+
+// What the last mgb_step_prepare computed into a step workspace (used to
+// reject a fused step whose coefficients were prepared for another dt or
+// equation).
+struct PrepRecord {
+  const void* work = nullptr;
+  double dt = 0, alpha = 0;
+  double kappa[3] = {0, 0, 0};
+  int nfields = 0, integrator = -1, order = 0;
+  bool valid = false;
+};
 
 struct mgb_plan {
   mgb_grid grid;
@@ -18,7 +31,13 @@ struct mgb_plan {
   // [nn][nz] each (inverse pivots and modified upper diagonals).
   double* th_inv = nullptr;
   double* th_cp = nullptr;
+  // Fully spectral: per-mode inversion factors tux, tuz, rlap (double,
+  // 3 x rows*cols) and tux, tuz (float, 2 x rows*cols).
+  double* tab_d = nullptr;
+  float* tab_f = nullptr;
   int device = 0;
+  mutable std::mutex mu;
+  mutable PrepRecord prep;
 };
 
 namespace mgb {
@@ -62,6 +81,8 @@ struct EventTrack {
 int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist,
             int curr, double dt, void* work, double* diag, cudaStream_t s, EventTrack* et = nullptr);
 size_t fs_step_workspace(const mgb_plan* p, int nfields);
+int fs_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void* work, cudaStream_t s);
+int fs_plan_init(mgb_plan* p);
 
 // ---- Fourier-x / Dirichlet-z family (fdm.cu) ----
 int fd_to_physical(const mgb_plan* p, const zd* spec, double* phys, cudaStream_t s);

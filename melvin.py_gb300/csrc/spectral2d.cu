@@ -1,4 +1,6 @@
 // Host orchestration of the fully spectral (doubly periodic) kernels.
+#include <vector>
+
 #include "spectral2d_impl.cuh"
 
 namespace mgb {
@@ -37,6 +39,18 @@ static int launched(cudaError_t e, const char* what) {
   return MGB_OK;
 }
 
+static void set_tables(const mgb_plan* p, XinvArgs& xa, bool split) {
+  const size_t S = (size_t)p->g.rows * p->g.cols;
+  if (split) {
+    xa.tux = p->tab_f;
+    xa.tuz = p->tab_f + S;
+  } else {
+    xa.tux = p->tab_d;
+    xa.tuz = p->tab_d + S;
+  }
+  xa.rlap = p->tab_d + 2 * S;
+}
+
 int fs_to_physical(const mgb_plan* p, const zd* spec, double* phys, void* work, cudaStream_t s) {
   const GridC& g = p->g;
   const FsLaunchers* Lx = fs_launchers(g.nx);
@@ -45,6 +59,7 @@ int fs_to_physical(const mgb_plan* p, const zd* spec, double* phys, void* work, 
   xa.g = g;
   xa.ld = g.cols;
   xa.tw = p->tw_x_d;
+  set_tables(p, xa, false);
   xa.job[0] = XinvJob{spec, SRC_COPY, work, nullptr, nullptr};
   int st = launched(Lx->xinv[0](xa, 1, s), "to_physical x pass");
   if (st) return st;
@@ -92,6 +107,7 @@ int fs_vec_dot_nabla(const mgb_plan* p, const zd* q, double* q_phys, const doubl
   xa.g = g;
   xa.ld = g.cols;
   xa.tw = p->tw_x_d;
+  set_tables(p, xa, false);
   xa.job[0] = XinvJob{q, SRC_COPY, w0, nullptr, nullptr};
   int st = launched(Lx->xinv[0](xa, 1, s), "vec_dot_nabla x pass");
   if (st) return st;
@@ -131,6 +147,7 @@ int fs_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* ux_s, zd* uz_s, dou
   xa.g = g;
   xa.ld = g.cols;
   xa.tw = p->tw_x_d;
+  set_tables(p, xa, false);
   xa.job[0] = XinvJob{w, SRC_UX, w0, ux_s, psi};
   xa.job[1] = XinvJob{w, SRC_UZ, w1, uz_s, nullptr};
   int st = launched(Lx->xinv[0](xa, 2, s), "velocity x pass");
@@ -146,30 +163,125 @@ int fs_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* ux_s, zd* uz_s, dou
   return launched(Lz->zinv_phys[1](za, s), "velocity z pass");
 }
 
-size_t fs_step_workspace(const mgb_plan* p, int nfields) {
+static inline size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Step scratch: transform intermediates, diagnostics partials, per-field
+// update coefficients (a, b) per mode.
+struct FsWork {
+  char* inter[6];
+  double* partial;
+  zd* coef[3];
+  size_t bytes;
+};
+
+static FsWork fs_carve(const mgb_plan* p, int F, void* base) {
   const bool split = p->grid.precision == MGB_PREC_SPLIT;
-  const int nin = 2 + nfields, nout = 2 * nfields;
+  const int nin = 2 + F, nout = 2 * F;
   const int ninter = nin > nout ? nin : nout;
-  return (size_t)ninter * inter_bytes(p->g, split) + (size_t)(p->g.nx / 2) * 3 * sizeof(double) + 256;
+  const size_t ib = al256(inter_bytes(p->g, split));
+  FsWork w = {};
+  char* c = (char*)base;
+  size_t off = 0;
+  for (int i = 0; i < 6; ++i) w.inter[i] = c + (size_t)(i < ninter ? i : ninter - 1) * ib;
+  off = (size_t)ninter * ib;
+  w.partial = (double*)(c + off);
+  off += al256((size_t)(p->g.nx / 2) * 3 * sizeof(double));
+  for (int f = 0; f < 3; ++f) {
+    w.coef[f] = (zd*)(c + off);
+    if (f < F) off += al256((size_t)p->g.rows * p->g.cols * sizeof(zd));
+  }
+  w.bytes = off;
+  return w;
 }
+
+size_t fs_step_workspace(const mgb_plan* p, int nfields) { return fs_carve(p, nfields, nullptr).bytes; }
+
+// Per-mode update coefficients of one field, with L = kappa * lap(n, m):
+//   semi-implicit (melvin/Integrator.py:58-63):
+//     a = (1 + (1-alpha) dt L) / (1 - alpha dt L),  b = c_AB / (1 - alpha dt L)
+//   explicit (melvin/Integrator.py:53-56):  a = L,  b = c_AB
+// with c_AB = dt/2 (AB2) or dt/24 (AB4).
+__global__ void k_update_coefs(GridC g, double kappa, int semi, double dt, double alpha, double cab,
+                               zd* __restrict__ out) {
+  const size_t total = (size_t)g.rows * g.cols;
+  for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < total; i += (size_t)gridDim.x * NT) {
+    const int r = (int)(i / g.cols), m = (int)(i - (size_t)r * g.cols);
+    const int n = row_mode(r, g.nn);
+    const double L = kappa * lap_symbol(g, n, m);
+    if (semi) {
+      const double c1 = 1 + ((1 - alpha) * dt) * L;
+      const double den = 1 - (alpha * dt) * L;
+      out[i] = mk(c1 / den, cab / den);
+    } else {
+      out[i] = mk(L, cab);
+    }
+  }
+}
+
+int fs_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void* work, cudaStream_t s) {
+  const GridC& g = p->g;
+  FsWork w = fs_carve(p, eq->nfields, work);
+  const double cab = eq->order == 2 ? dt / 2 : dt / 24;
+  const size_t total = (size_t)g.rows * g.cols;
+  size_t nb = (total + NT - 1) / NT;
+  nb = nb > 152 * 8 ? 152 * 8 : nb;
+  for (int f = 0; f < eq->nfields; ++f) {
+    k_update_coefs<<<(int)nb, NT, 0, s>>>(g, eq->f[f].kappa, eq->integrator == MGB_INT_SEMI_IMPLICIT ? 1 : 0, dt,
+                                          eq->alpha, cab, w.coef[f]);
+    MGB_LAUNCH_CHECK();
+  }
+  return MGB_OK;
+}
+
+int fs_plan_init(mgb_plan* p) {
+  const GridC& g = p->g;
+  const size_t S = (size_t)g.rows * g.cols;
+  std::vector<double> td(3 * S);
+  std::vector<float> tf(2 * S);
+  for (int r = 0; r < g.rows; ++r) {
+    const int n = row_mode(r, g.nn);
+    for (int m = 0; m < g.cols; ++m) {
+      const size_t i = (size_t)r * g.cols + m;
+      const double a = g.d2x * (double)(n * n);
+      const double b = g.d2z * (double)(m * m);
+      const double lap = (i == 0) ? 1.0 : a + b;
+      const double tux = (g.dfz * (double)m) / lap;
+      const double tuz = (g.dfx * (double)n) / lap;
+      td[i] = tux;
+      td[S + i] = tuz;
+      td[2 * S + i] = 1.0 / lap;
+      tf[i] = (float)tux;
+      tf[S + i] = (float)tuz;
+    }
+  }
+  MGB_CUDA(cudaMalloc(&p->tab_d, td.size() * sizeof(double)));
+  MGB_CUDA(cudaMalloc(&p->tab_f, tf.size() * sizeof(float)));
+  MGB_CUDA(cudaMemcpy(p->tab_d, td.data(), td.size() * sizeof(double), cudaMemcpyHostToDevice));
+  MGB_CUDA(cudaMemcpy(p->tab_f, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return MGB_OK;
+}
+
 
 int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist, int curr,
             double dt, void* work, double* diag, cudaStream_t s, EventTrack* et) {
   EventTrack none;
   if (!et) et = &none;
-  et->mark(s);
   const GridC& g = p->g;
   const int F = eq->nfields;
+  {
+    // the update coefficients in `work` must be the ones for (eq, dt)
+    std::lock_guard<std::mutex> lock(p->mu);
+    const PrepRecord& pr = p->prep;
+    bool ok = pr.valid && pr.work == work && pr.dt == dt && pr.nfields == F && pr.integrator == eq->integrator &&
+              pr.order == eq->order && (eq->integrator != MGB_INT_SEMI_IMPLICIT || pr.alpha == eq->alpha);
+    for (int f = 0; ok && f < F; ++f) ok = pr.kappa[f] == eq->f[f].kappa;
+    if (!ok) return fail(MGB_ERR_INVALID, "mgb_step: call mgb_step_prepare for this equation, dt and workspace first");
+  }
+  et->mark(s);
   const int split = p->grid.precision == MGB_PREC_SPLIT ? 1 : 0;
   const FsLaunchers* Lx = fs_launchers(g.nx);
   const FsLaunchers* Lz = fs_launchers(g.nz);
-  const size_t ib = inter_bytes(g, split);
-  const int nin = 2 + F, nout = 2 * F;
-  const int ninter = nin > nout ? nin : nout;
-  char* inter[6];
-  for (int i = 0; i < 6; ++i) inter[i] = (char*)work + (size_t)i * ib;
-  double* partial = (double*)((char*)work + (size_t)ninter * ib);
-  partial = (double*)(((uintptr_t)partial + 255) & ~(uintptr_t)255);
+  FsWork w = fs_carve(p, F, work);
   const void* twx = split ? p->tw_x_f : p->tw_x_d;
   const void* twz = split ? p->tw_z_f : p->tw_z_d;
 
@@ -177,9 +289,10 @@ int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* con
   xa.g = g;
   xa.ld = g.cols;
   xa.tw = twx;
-  xa.job[0] = XinvJob{(const zd*)q[0], SRC_UX, inter[0], nullptr, nullptr};
-  xa.job[1] = XinvJob{(const zd*)q[0], SRC_UZ, inter[1], nullptr, nullptr};
-  for (int f = 0; f < F; ++f) xa.job[2 + f] = XinvJob{(const zd*)q[f], SRC_COPY, inter[2 + f], nullptr, nullptr};
+  set_tables(p, xa, split);
+  xa.job[0] = XinvJob{(const zd*)q[0], SRC_UX, w.inter[0], nullptr, nullptr};
+  xa.job[1] = XinvJob{(const zd*)q[0], SRC_UZ, w.inter[1], nullptr, nullptr};
+  for (int f = 0; f < F; ++f) xa.job[2 + f] = XinvJob{(const zd*)q[f], SRC_COPY, w.inter[2 + f], nullptr, nullptr};
   int st = launched(Lx->xinv[split](xa, 2 + F, s), "step x pass");
   if (st) return st;
   et->mark(s);
@@ -187,12 +300,12 @@ int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* con
   ZzArgs za = {};
   za.g = g;
   za.ld = g.cols;
-  for (int i = 0; i < 2 + F; ++i) za.in[i] = inter[i];
+  for (int i = 0; i < 2 + F; ++i) za.in[i] = w.inter[i];
   for (int f = 0; f < F; ++f) {
-    za.aout[f] = inter[f];
-    za.cout[f] = inter[F + f];
+    za.aout[f] = w.inter[f];
+    za.cout[f] = w.inter[F + f];
   }
-  za.partial = diag ? partial : nullptr;
+  za.partial = diag ? w.partial : nullptr;
   za.fdz = fd_inv(g.sdo, g.dz);
   za.tw = twz;
   st = launched(Lz->zz_step[split][F - 1](za, s), "step z pass");
@@ -203,13 +316,14 @@ int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* con
   fa.g = g;
   fa.ld = g.cols;
   fa.need_psi = 0;
+  fa.rlap = p->tab_d + 2 * (size_t)g.rows * g.cols;
   for (int f = 0; f < F; ++f) {
-    fa.ain[f] = inter[f];
-    fa.cin[f] = inter[F + f];
+    fa.ain[f] = w.inter[f];
+    fa.cin[f] = w.inter[F + f];
     fa.q[f] = (zd*)q[f];
     fa.hist[f] = (zd*)hist[f];
+    fa.coef[f] = w.coef[f];
     const mgb_field_eq& fe = eq->f[f];
-    fa.eq[f].kappa = fe.kappa;
     fa.eq[f].nterms = fe.nterms;
     fa.eq[f].bc = fe.bc;
     for (int t = 0; t < fe.nterms; ++t) {
@@ -222,15 +336,13 @@ int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* con
   fa.order = eq->order;
   fa.curr = curr;
   fa.integrator = eq->integrator;
-  fa.dt = dt;
-  fa.alpha = eq->alpha;
   fa.fdx = fd_inv(g.sdo, g.dx);
   fa.inv_norm = 1.0 / ((double)g.nx * (double)g.nz);
   fa.tw = twx;
   st = launched(Lx->xf_step[split][F - 1](fa, s), "step forward x pass");
   if (st) return st;
   et->mark(s);
-  if (diag) return pw_finish_diag(partial, g.nx / 2, 1.0 / ((double)g.nx * (double)g.nz), diag, s);
+  if (diag) return pw_finish_diag(w.partial, g.nx / 2, 1.0 / ((double)g.nx * (double)g.nz), diag, s);
   return MGB_OK;
 }
 

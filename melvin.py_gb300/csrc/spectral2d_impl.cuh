@@ -58,14 +58,22 @@ struct XinvJob {
   const zd* src;  // spectral state
   int kind;       // SrcKind
   void* out;      // intermediate [nx][ld]
-  zd* spec_out;   // optional: the derived spectral field (ux_s / uz_s)
-  zd* psi_out;    // optional: psi = solve(-src)
+  zd* spec_out;   // optional (FP64 kernels): the derived spectral field (ux_s / uz_s)
+  zd* psi_out;    // optional (FP64 kernels): psi = solve(-src)
 };
 
+// Per-mode factors of the streamfunction inversion, precomputed per plan
+// (lap(0,0) := 1, melvin/LaplacianSolver.py:58-68):
+//   tux = (2 pi/lz) m / lap,  tuz = (2 pi/lx) n / lap,  rlap = 1 / lap,
+// so that ux = -(2 pi i/lz) m psi = i tux w and uz = (2 pi i/lx) n psi =
+// -i tuz w with psi = -w / lap (melvin/utility.py:62-79).
 struct XinvArgs {
   GridC g;
   XinvJob job[5];
   int ld;
+  const void* tux;     // T[rows*cols]
+  const void* tuz;     // T[rows*cols]
+  const double* rlap;  // double[rows*cols]
   const void* tw;
 };
 
@@ -77,31 +85,29 @@ __global__ void __launch_bounds__(NT) k_xinv(const XinvArgs a) {
   const GridC& g = a.g;
   const XinvJob jb = a.job[blockIdx.y];
   const int m0 = blockIdx.x * C;
+  const T* tab = (const T*)(jb.kind == SRC_UX ? a.tux : a.tuz);
   for (int e = threadIdx.x; e < N * C; e += NT) buf[e] = mk<T>(0, 0);
   __syncthreads();
   for (int e = threadIdx.x; e < g.rows * C; e += NT) {
     const int r = e / C, c = e - r * C, m = m0 + c;
     if (m >= g.cols) continue;
     const size_t idx = (size_t)r * g.cols + m;
-    zd v = jb.src[idx];
-    if (jb.kind != SRC_COPY) {
-      // psi = -w / lap with lap(0,0) := 1 (melvin/LaplacianSolver.py:58-68)
-      const int n = row_mode(r, g.nn);
-      const double lap = (idx == 0) ? 1.0 : lap_symbol(g, n, m);
-      const zd psi = mk(-v.x / lap, -v.y / lap);
-      if (jb.psi_out) jb.psi_out[idx] = psi;
-      if (jb.kind == SRC_UX) {
-        // ux = -(2*pi*i/lz) m psi  (melvin/utility.py:70)
-        const double b = g.dfz * (double)m;
-        v = mk(b * psi.y, -(b * psi.x));
-      } else {
-        // uz = (2*pi*i/lx) n psi  (melvin/utility.py:77)
-        const double b = g.dfx * (double)n;
-        v = mk(-(b * psi.y), b * psi.x);
-      }
+    const zd w = jb.src[idx];
+    const cx<T> wt = cvt<T>(w);
+    cx<T> v = wt;
+    if (jb.kind == SRC_UX) {
+      const T t = tab[idx];
+      v = mk(-(t * wt.y), t * wt.x);
+    } else if (jb.kind == SRC_UZ) {
+      const T t = tab[idx];
+      v = mk(t * wt.y, -(t * wt.x));
     }
-    if (jb.spec_out) jb.spec_out[idx] = v;
-    buf[row_bin(r, g.nn, N) * C + c] = mk((T)v.x, (T)v.y);
+    if (jb.spec_out) jb.spec_out[idx] = cvt<double>(v);
+    if (jb.psi_out) {
+      const double rl = a.rlap[idx];
+      jb.psi_out[idx] = mk(-(w.x * rl), -(w.y * rl));
+    }
+    buf[row_bin(r, g.nn, N) * C + c] = v;
   }
   __syncthreads();
   block_fft<T, N, C, C, NT, +1>(buf, (const cx<T>*)a.tw);
@@ -304,7 +310,6 @@ __global__ void __launch_bounds__(NT) k_zz_step(const ZzArgs a) {
 // ---------------------------------------------------------------------------
 
 struct XfField {
-  double kappa;
   int nterms;
   int tsrc[4];
   int top[4];
@@ -319,8 +324,10 @@ struct XfArgs {
   const void* cin[3];
   zd* q[3];
   zd* hist[3];
+  const zd* coef[3];   // per-mode update coefficients (a, b) from mgb_step_prepare
+  const double* rlap;  // 1/lap, for linear terms of psi
   int order, curr, integrator, need_psi;
-  double dt, alpha, fdx, inv_norm;
+  double fdx, inv_norm;
   XfField eq[3];
   const void* tw;
 };
@@ -355,20 +362,18 @@ __device__ __forceinline__ zd lin_term(const GridC& g, zd s, int op, int n, int 
   return s;
 }
 
-// Adams-Bashforth combination (melvin/Integrator.py:5-18) given f0.
-__device__ __forceinline__ zd adams_bashforth(const zd* h, size_t slot, int order, int curr, zd f0,
-                                              double dt) {
+// Weighted Adams-Bashforth sum 3 f0 - f1 (AB2) or
+// 55 f0 - 59 f1 + 37 f2 - 9 f3 (AB4) (melvin/Integrator.py:5-18); the dt/2
+// or dt/24 factor is part of the update coefficients.
+__device__ __forceinline__ zd ab_sum(const zd* h, size_t slot, int order, int curr, zd f0) {
   if (order == 2) {
     const zd f1 = h[(size_t)((curr + 1) & 1) * slot];
-    const double c = dt / 2;
-    return mk(c * (3 * f0.x - f1.x), c * (3 * f0.y - f1.y));
+    return mk(3 * f0.x - f1.x, 3 * f0.y - f1.y);
   }
   const zd f1 = h[(size_t)((curr + 3) & 3) * slot];
   const zd f2 = h[(size_t)((curr + 2) & 3) * slot];
   const zd f3 = h[(size_t)((curr + 1) & 3) * slot];
-  const double c = dt / 24;
-  return mk(c * (((55 * f0.x - 59 * f1.x) + 37 * f2.x) - 9 * f3.x),
-            c * (((55 * f0.y - 59 * f1.y) + 37 * f2.y) - 9 * f3.y));
+  return mk(((55 * f0.x - 59 * f1.x) + 37 * f2.x) - 9 * f3.x, ((55 * f0.y - 59 * f1.y) + 37 * f2.y) - 9 * f3.y);
 }
 
 template <typename T, int N, int F>
@@ -393,6 +398,8 @@ __global__ void __launch_bounds__(NT) k_xf_step(const XfArgs a) {
 #pragma unroll
   for (int f = 0; f < F; ++f) block_fft<T, N, C, C, NT, -1>(buf + f * N * C, (const cx<T>*)a.tw);
 
+  // -1/(nx*nz) is a power of two for the grids built, so scaling in T is exact
+  const T neg_norm = (T)(-a.inv_norm);
   const size_t slot = (size_t)g.rows * g.cols;
   for (int e = threadIdx.x; e < g.rows * C; e += NT) {
     const int r = e / C, c = e - r * C, m = m0 + c;
@@ -402,18 +409,17 @@ __global__ void __launch_bounds__(NT) k_xf_step(const XfArgs a) {
     zd qo[F];
 #pragma unroll
     for (int f = 0; f < F; ++f) qo[f] = a.q[f][idx];
-    const double lap0 = lap_symbol(g, n, m);
     zd psi = mk(0.0, 0.0);
     if (a.need_psi) {
-      const double l1 = (idx == 0) ? 1.0 : lap0;
-      psi = mk(-qo[0].x / l1, -qo[0].y / l1);
+      const double rl = a.rlap[idx];
+      psi = mk(-(qo[0].x * rl), -(qo[0].y * rl));
     }
 #pragma unroll
     for (int f = 0; f < F; ++f) {
       const XfField& eq = a.eq[f];
-      const cx<T> J = buf[f * N * C + k * C + c];
       // dq[:] = -q.vec_dot_nabla(...) + linear terms
-      zd fv = mk(-((double)J.x * a.inv_norm), -((double)J.y * a.inv_norm));
+      const cx<T> J = buf[f * N * C + k * C + c] * neg_norm;
+      zd fv = cvt<double>(J);
       for (int t = 0; t < eq.nterms; ++t) {
         const int sidx = eq.tsrc[t];
         zd s = psi;
@@ -423,20 +429,19 @@ __global__ void __launch_bounds__(NT) k_xf_step(const XfArgs a) {
         const zd v = lin_term(g, s, eq.top[t], n, m);
         fv = mk(fv.x + eq.tcoef[t] * v.x, fv.y + eq.tcoef[t] * v.y);
       }
-      const double L = eq.kappa * lap0;
+      const zd cf = a.coef[f][idx];
       zd qn;
       if (a.integrator == MGB_INT_SEMI_IMPLICIT) {
+        // q' = ((1 + (1-a) dt L) q + AB) / (1 - a dt L) = cf.x q + cf.y * sum
         a.hist[f][(size_t)a.curr * slot + idx] = fv;
-        const zd ab = adams_bashforth(a.hist[f] + idx, slot, a.order, a.curr, fv, a.dt);
-        const double c1 = 1 + ((1 - a.alpha) * a.dt) * L;
-        const double den = 1 - (a.alpha * a.dt) * L;
-        qn = mk((c1 * qo[f].x + ab.x) / den, (c1 * qo[f].y + ab.y) / den);
+        const zd sm = ab_sum(a.hist[f] + idx, slot, a.order, a.curr, fv);
+        qn = mk(cf.x * qo[f].x + cf.y * sm.x, cf.x * qo[f].y + cf.y * sm.y);
       } else {
-        // explicit: the history keeps N + D with D = kappa * snabla2(q)
-        fv = mk(fv.x + L * qo[f].x, fv.y + L * qo[f].y);
+        // explicit: the history keeps N + D, D = kappa * snabla2(q) = cf.x q
+        fv = mk(fv.x + cf.x * qo[f].x, fv.y + cf.x * qo[f].y);
         a.hist[f][(size_t)a.curr * slot + idx] = fv;
-        const zd ab = adams_bashforth(a.hist[f] + idx, slot, a.order, a.curr, fv, a.dt);
-        qn = mk(qo[f].x + ab.x, qo[f].y + ab.y);
+        const zd sm = ab_sum(a.hist[f] + idx, slot, a.order, a.curr, fv);
+        qn = mk(qo[f].x + cf.y * sm.x, qo[f].y + cf.y * sm.y);
       }
       if ((eq.bc & MGB_BC_ZERO_M0) && m == 0) qn = mk(0.0, 0.0);
       a.q[f][idx] = qn;
@@ -603,9 +608,12 @@ __global__ void __launch_bounds__(NT) k_xf_out(const XfOutArgs a) {
 // Launchers (one instantiation set per transform length N).
 // ---------------------------------------------------------------------------
 
+// Opt in to more than the default 48 KB of shared memory per CTA.  Kernels
+// here use at most 1 KB of static shared memory, so any dynamic request
+// above 47 KB opts in.
 template <typename K>
 inline cudaError_t prep_smem(K kernel, size_t smem) {
-  if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 47 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   return cudaSuccess;
 }
 

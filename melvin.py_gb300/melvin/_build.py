@@ -27,7 +27,8 @@ LIB_DIR = PKG_DIR / "_lib"
 LIB_NAME = "libmelvin_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INCLUDE}", f"-I{CSRC}"]
+# -ffp-contract=off keeps host-side table arithmetic identical on x86 and Arm
+CFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
 
 
 def nvcc() -> str:

@@ -113,6 +113,7 @@ SIGNATURES = {
     "mgb_adams": [_P, _I, _P, _I, _I, _D, _P, _P],
     "mgb_diagnostics": [_P, _P, _P, _P, _P, _P],
     "mgb_step": [_P, C.POINTER(MgbEquation), C.POINTER(_P), C.POINTER(_P), _I, _D, _P, _P, _P],
+    "mgb_step_prepare": [_P, C.POINTER(MgbEquation), _D, _P, _P],
     "mgb_step_kernel_count": [_P, C.POINTER(MgbEquation), C.POINTER(_I)],
     "mgb_step_events": [_P, C.POINTER(MgbEquation), C.POINTER(_P), C.POINTER(_P), _I, _D, _P, _P, _P,
                         C.POINTER(_P), _I],
@@ -187,6 +188,7 @@ class Plan:
         self.physical_shape = (pr.value, pc.value)
         self._work = None
         self._step_work = {}
+        self.last_prepared = None  # the Stepper whose coefficients the plan last prepared
 
     def workspace_bytes(self, family, nfields=1):
         b = C.c_size_t()

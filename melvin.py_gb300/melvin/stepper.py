@@ -78,12 +78,25 @@ class Stepper:
         self.diag = torch.zeros(3, dtype=torch.float64, device=self.device)
         self._q = (C.c_void_p * 3)()
         self._h = (C.c_void_p * 3)()
+        self._prepared_dt = None
+
+    def prepare(self, dt):
+        """(Re)compute the per-mode update coefficients for `dt`."""
+        self.plan.call("mgb_step_prepare", C.byref(self.eq), float(dt), N.ptr(self.work),
+                       N.stream_handle(self.device))
+        self._prepared_dt = float(dt)
+
+    def _ensure(self, dt):
+        if self._prepared_dt != float(dt) or self.plan.last_prepared is not self:
+            self.prepare(dt)
+            self.plan.last_prepared = self
 
     def step(self, dt=None, diagnostics=False):
         """Advance every field by one step; returns the device tensor
         (kinetic energy, max ux, max uz) of the start-of-step velocity when
         `diagnostics` is set."""
         dt = self.sim._integrator._dt if dt is None else dt
+        self._ensure(dt)
         curr = self.fields[0].dvar._curr_idx
         for i, f in enumerate(self.fields):
             if f.dvar._curr_idx != curr:
@@ -108,6 +121,7 @@ class Stepper:
         ``events[k]`` after kernel k (torch.cuda.Event objects, already
         recorded once so that they exist)."""
         dt = self.sim._integrator._dt if dt is None else dt
+        self._ensure(dt)
         curr = self.fields[0].dvar._curr_idx
         for i, f in enumerate(self.fields):
             self._q[i] = f.var._sdata.data_ptr()

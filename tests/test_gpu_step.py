@@ -168,3 +168,51 @@ def test_split_precision_close_to_fp64(cuda, golden, tag):
     for n in names:
         err = rel_l2(V[n].gets().cpu().numpy(), golden[f"{tag}/s{nsteps}_{n}"])
         assert err < 1e-5, (n, err)
+
+
+@pytest.mark.parametrize(
+    "nx,nz,fdm,precision,integ,order,tol",
+    [(2048, 2048, False, "double", "semi-implicit", 2, TOL),
+     (2048, 2048, False, "split", "semi-implicit", 2, 1e-5),
+     (4096, 256, False, "double", "semi-implicit", 4, TOL),
+     (1024, 513, True, "double", "pece", 4, TOL),
+     (1024, 513, True, "split", "pece", 4, 1e-5),
+     (1024, 1025, True, "split", "explicit", 2, 1e-5)],
+)
+def test_fused_step_large_grids(cuda, nx, nz, fdm, precision, integ, order, tol):
+    """One fused step at the benchmark grid sizes against the oracle
+    (shared-memory footprints, grid shapes and tile edges of the big
+    configurations)."""
+    import melvin
+    from melvin import BasisFunctions as B, equations, workloads
+
+    lx, lz = (2 * np.pi, 2 * np.pi) if not fdm else (2.0, 1.0)
+    sdo = 4 if order == 4 else 2
+    g = O.Grid(nx, nz, lx, lz, fdm, sdo)
+    p = melvin.Parameters(params_dict(g, "explicit" if integ == "pece" else integ, order, 1e-7 if fdm else 2e-4,
+                                      precision))
+    sim = melvin.Simulation(p, torch)
+    bf = [B.COMPLEX_EXP, B.FDM if fdm else B.COMPLEX_EXP]
+    if fdm:
+        w, dw, t, dt_ = sim.make_variable("w", bf), sim.make_derivative("dw"), sim.make_variable("t", bf), \
+            sim.make_derivative("dt")
+        t0 = workloads.conductive(nx, nz, lx, lz, seed=3)
+        t.load(t0, is_physical=True)
+        step = equations.rayleigh_benard(sim, w, dw, t, dt_, 1.0, 1e7, integrator=integ)
+        ref = P.Problem(g, P.rbc_specs(1.0, 1e7), [np.zeros(g.spectral_shape, complex), O.to_spectral(g, t0)],
+                        1e-7, integ, order)
+        for _ in range(2):
+            step.step()
+            ref.step()
+        assert rel_l2(w.gets().cpu().numpy(), ref.q[0]) < tol
+        assert rel_l2(t.gets().cpu().numpy(), ref.q[1]) < tol
+    else:
+        w, dw = sim.make_variable("w", bf), sim.make_derivative("dw")
+        w0 = workloads.decaying_turbulence(nx, nz, seed=1)
+        w.load(w0, is_physical=True)
+        step = equations.vorticity(sim, w, dw, 5e-5)
+        ref = P.Problem(g, P.vorticity_specs(5e-5), [O.to_spectral(g, w0)], 2e-4, "semi-implicit", order)
+        for _ in range(2):
+            step.step()
+            ref.step()
+        assert rel_l2(w.gets().cpu().numpy(), ref.q[0]) < tol
