@@ -200,24 +200,24 @@ def kernel_model(n, split):
     }
 
 
-def timed_steps(step, steps, flush, with_kernels=True):
-    """Run `steps` fused steps; each bracketed by CUDA events on the launching
-    stream, with an L2 flush (untimed) between steps.  Returns per-step ms
-    and per-kernel ms lists."""
+def timed_steps(step, steps, flush):
+    """Run `steps` fused steps, each bracketed by CUDA events recorded on the
+    launching stream (per-kernel events inside the step), with an L2 flush
+    between steps outside the events.  Returns per-step and per-kernel ms."""
     import torch
 
     nk = step.kernel_count()
-    per_step, per_kernel = [], [[] for _ in range(nk)]
+    evs = []
     for _ in range(steps):
         flush.zero_()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(nk + 1)]
         for e in ev:
             e.record()  # materialise the events
         step.step_events(ev)
-        torch.cuda.synchronize()
-        per_step.append(ev[0].elapsed_time(ev[-1]))
-        for k in range(nk):
-            per_kernel[k].append(ev[k].elapsed_time(ev[k + 1]))
+        evs.append(ev)
+    torch.cuda.synchronize()
+    per_step = [ev[0].elapsed_time(ev[-1]) for ev in evs]
+    per_kernel = [[ev[k].elapsed_time(ev[k + 1]) for ev in evs] for k in range(nk)]
     return per_step, per_kernel
 
 
@@ -313,7 +313,7 @@ def run_only(args):
     n = args.n
     w0 = workloads.decaying_turbulence(n, n, seed=0)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
-    sim, w, dw, step = make_run(n, "split" if args.only == "split" else "double", device, w0)
+    sim, w, dw, step = make_run(n, {"fp64": "double"}.get(args.only, args.only), device, w0)
     for _ in range(args.warmup):
         step.step()
     torch.cuda.synchronize()
@@ -324,8 +324,45 @@ def run_only(args):
     return 0
 
 
-def run_native(args):
+def _timed_run(n, precision, device, w0, steps, warmup, flush, dist):
+    """Warm up, then time `steps` fused steps of one precision; returns the
+    per-step and per-kernel times and the stepper."""
+    import torch
+
+    sim, w, dw, step = make_run(n, precision, device, w0)
+    for _ in range(warmup):
+        step.step()
+    torch.cuda.synchronize()
+    barrier(dist)
+    torch.cuda.synchronize()
+    per_step, per_kernel = timed_steps(step, steps, flush)
+    torch.cuda.synchronize()
+    barrier(dist)
+    return per_step, per_kernel, (sim, w, dw, step)
+
+
+def _accuracy(n, device, w0, precision, nsteps=100):
+    """Relative L2 of the state against the FP64 path after 1 and `nsteps`
+    steps from the same initial field, and the max relative error of the
+    kinetic-energy trajectory."""
     import numpy as np
+    import torch
+
+    _, wa, _, sa = make_run(n, "double", device, w0)
+    _, wb, _, sb = make_run(n, precision, device, w0)
+    ke_a, ke_b, out = [], [], {}
+    for k in range(1, nsteps + 1):
+        ke_a.append(float(sa.step(diagnostics=True)[0]))
+        ke_b.append(float(sb.step(diagnostics=True)[0]))
+        if k in (1, nsteps):
+            err = (torch.linalg.vector_norm(wa._sdata - wb._sdata) / torch.linalg.vector_norm(wa._sdata)).item()
+            out["rel_l2_1step" if k == 1 else f"rel_l2_{nsteps}steps"] = err
+    ke_a, ke_b = np.array(ke_a), np.array(ke_b)
+    out["ke_traj_max_rel_err"] = float(np.max(np.abs(ke_b - ke_a) / np.abs(ke_a)))
+    return out
+
+
+def run_native(args):
     import torch
 
     from melvin import workloads
@@ -340,82 +377,46 @@ def run_native(args):
     peak, peak_kind = load_peaks()
     traffic = load_traffic()
     names = ["xinv", "zstep", "xfwd"]
-
-    # ---- plain FP64 ----
-    sim, w, dw, step = make_run(n, "double", device, w0)
-    for _ in range(args.warmup):
-        step.step()
-    torch.cuda.synchronize()
-    barrier(dist)
-    torch.cuda.synchronize()
-    t_wall0 = time.perf_counter()
+    results = {}
     with ClockSampler(local) as clocks:
-        per_step, per_kernel = timed_steps(step, args.steps, flush)
-    torch.cuda.synchronize()
-    barrier(dist)
-    wall = time.perf_counter() - t_wall0
-    secs = sum(per_step) * 1e-3
-    max_secs = reduce_max(secs, dist, device)
-    value = aggregate_throughput(n * n, args.steps, world, max_secs)
-    model = kernel_model(n, False)
-    roof, kdom = roofline(model, per_kernel, names, peak, peak_kind, traffic, "double")
-    avg_k = [statistics.mean(v) for v in per_kernel]
-    flops = [model[k]["flops"] for k in names]
-    fp64 = {
-        "kernel": names[kdom], "achieved_tflops": round(flops[kdom] / (avg_k[kdom] * 1e-3) / 1e12, 4),
-        "peak_tflops": FP64_FMA_TFLOPS, "frac": round(flops[kdom] / (avg_k[kdom] * 1e-3) / 1e12 / FP64_FMA_TFLOPS, 4),
-        "note": "nominal 5 N log2 N flops per complex FFT; peak = measured FP64 FMA rate of this GB300",
-    }
+        t_wall0 = time.perf_counter()
+        for key, prec in (("fp64", "double"), ("split", "split"), ("dfloat", "dfloat")):
+            per_step, per_kernel, run = _timed_run(n, prec, device, w0, args.steps, args.warmup, flush, dist)
+            secs = reduce_max(sum(per_step) * 1e-3, dist, device)
+            model = kernel_model(n, prec == "split")
+            roof, kdom = roofline(model, per_kernel, names, peak, peak_kind, traffic, prec)
+            results[key] = dict(secs=secs, per_kernel=per_kernel, roof=roof, kdom=kdom, model=model, run=run,
+                                value=aggregate_throughput(n * n, args.steps, world, secs))
+            if key == "fp64":
+                wall = time.perf_counter() - t_wall0
 
-    # ---- end to end through the public API with host buffers ----
-    h_w = torch.empty_like(w._sdata, device="cpu").pin_memory()
-    h_dw = torch.empty_like(dw._data, device="cpu").pin_memory()
-    h_w.copy_(w._sdata)
-    h_dw.copy_(dw._data)
-    e2e_ms = []
-    for _ in range(args.steps):
-        flush.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        w._sdata.copy_(h_w, non_blocking=True)
-        dw._data.copy_(h_dw, non_blocking=True)
-        step.step()
-        h_w.copy_(w._sdata, non_blocking=True)
-        h_dw.copy_(dw._data, non_blocking=True)
-        e1.record()
+        # end to end through the public API with host buffers (FP64)
+        sim, w, dw, step = results["fp64"]["run"]
+        h_w = torch.empty_like(w._sdata, device="cpu").pin_memory()
+        h_dw = torch.empty_like(dw._data, device="cpu").pin_memory()
+        h_w.copy_(w._sdata)
+        h_dw.copy_(dw._data)
+        e2e_ev = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            w._sdata.copy_(h_w, non_blocking=True)
+            dw._data.copy_(h_dw, non_blocking=True)
+            step.step()
+            h_w.copy_(w._sdata, non_blocking=True)
+            h_dw.copy_(dw._data, non_blocking=True)
+            e1.record()
+            e2e_ev.append((e0, e1))
         torch.cuda.synchronize()
-        e2e_ms.append(e0.elapsed_time(e1))
-    e2e_secs = reduce_max(sum(e2e_ms) * 1e-3, dist, device)
-    io_bytes = (h_w.numel() + h_dw.numel()) * 16
+        e2e_secs = reduce_max(sum(a.elapsed_time(b) for a, b in e2e_ev) * 1e-3, dist, device)
+        io_bytes = (h_w.numel() + h_dw.numel()) * 16
 
-    # ---- split precision ----
-    sim_s, w_s, dw_s, step_s = make_run(n, "split", device, w0)
-    for _ in range(args.warmup):
-        step_s.step()
-    torch.cuda.synchronize()
-    per_step_s, per_kernel_s = timed_steps(step_s, args.steps, flush)
-    secs_s = reduce_max(sum(per_step_s) * 1e-3, dist, device)
-    value_s = aggregate_throughput(n * n, args.steps, world, secs_s)
-    roof_s, _ = roofline(kernel_model(n, True), per_kernel_s, names, peak, peak_kind, traffic, "split")
-
-    # ---- split-precision error against the FP64 path (same initial field) ----
     acc = {}
     if rank == 0:
-        _, wa, _, sa = make_run(n, "double", device, w0)
-        _, wb, _, sb = make_run(n, "split", device, w0)
-        ke_a, ke_b = [], []
-        for k in range(1, 101):
-            da = sa.step(diagnostics=True)
-            db = sb.step(diagnostics=True)
-            ke_a.append(float(da[0]))
-            ke_b.append(float(db[0]))
-            if k in (1, 100):
-                err = (torch.linalg.vector_norm(wa._sdata - wb._sdata) / torch.linalg.vector_norm(wa._sdata)).item()
-                acc[f"rel_l2_{k}step" + ("s" if k > 1 else "")] = err
-        ke_a, ke_b = np.array(ke_a), np.array(ke_b)
-        acc["ke_traj_max_rel_err"] = float(np.max(np.abs(ke_b - ke_a) / np.abs(ke_a)))
+        acc["split"] = _accuracy(n, device, w0, "split")
+        acc["dfloat"] = _accuracy(n, device, w0, "dfloat")
 
-    # ---- CPU baseline (rank 0, N = 1 only) ----
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, csecs = cpu_step_sample(w0, n, 2)
@@ -424,23 +425,34 @@ def run_native(args):
                          "core (pocketfft is single-threaded)"}
 
     if rank == 0:
-        ms = max_secs / args.steps * 1e3
+        r64 = results["fp64"]
+        avg_k = [statistics.mean(v) for v in r64["per_kernel"]]
+        kd = r64["kdom"]
+        fl = r64["model"][names[kd]]["flops"] / (avg_k[kd] * 1e-3) / 1e12
+        fp64_roof = {"kernel": names[kd], "achieved_tflops": round(fl, 4), "peak_tflops": FP64_FMA_TFLOPS,
+                     "frac": round(fl / FP64_FMA_TFLOPS, 4),
+                     "note": "nominal 5 N log2 N flops per complex FFT; peak = measured FP64 FMA rate of this GB300"}
+
+        def sub(key, dtype):
+            r = results[key]
+            return {"value": round(r["value"], 3), "unit": UNIT, "dtype": dtype,
+                    "ms_per_step": round(r["secs"] / args.steps * 1e3, 4),
+                    "speedup_vs_fp64": round(r["value"] / r64["value"], 3), "roofline": r["roof"], **acc[key]}
+
         line = {
-            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": DATA,
-            "config": dict(WORKLOAD, nx=n, nz=n, l2="flushed (256 MiB write) between timed steps",
-                           replicas=world),
-            "roofline": roof,
-            "fp64_alu_roof": fp64,
+            "metric": METRIC, "value": round(r64["value"], 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(r64["secs"] / args.steps * 1e3, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+            "config": dict(WORKLOAD, nx=n, nz=n, l2="flushed (256 MiB write) between timed steps", replicas=world),
+            "roofline": r64["roof"],
+            "fp64_alu_roof": fp64_roof,
             "e2e": {"value": round(aggregate_throughput(n * n, args.steps, world, e2e_secs), 3), "unit": UNIT,
                     "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
-                    "path": "Stepper.step with state and history copied from/to pinned host memory each step"},
-            "split": {"value": round(value_s, 3), "unit": UNIT, "dtype": "f32 transforms / f64 state",
-                      "ms_per_step": round(secs_s / args.steps * 1e3, 4),
-                      "speedup_vs_fp64": round(value_s / value, 3), "roofline": roof_s, **acc},
+                    "path": "Stepper.step (FP64) with state and history copied from/to pinned host memory each step"},
+            "split": sub("split", "f32 transforms / f64 state and history"),
+            "dfloat": sub("dfloat", "double-float (f32 pair) transforms / f64 state and history"),
             "cpu_baseline": cpu,
-            "gpu_launches": step.kernel_count() * args.steps,
+            "gpu_launches": results["fp64"]["run"][3].kernel_count() * args.steps,
             "clocks": clocks.summary(),
             "wall_s_fp64_timed": round(wall, 3),
         }
@@ -454,12 +466,13 @@ def run_native(args):
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
     ap.add_argument("--n", type=int, default=2048, help="grid points per side (default 2048)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--only", choices=["fp64", "split"], help="run only the timed fused steps of one precision")
+    ap.add_argument("--only", choices=["fp64", "split", "dfloat"],
+                    help="run only the timed fused steps of one precision")
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "native":
         ap.error("--warmup must be >= 3")

@@ -41,7 +41,9 @@ typedef enum mgb_status {
 
 typedef enum mgb_precision {
   MGB_PREC_DOUBLE = 0, /* FP64 transforms, derivatives and products */
-  MGB_PREC_SPLIT = 1   /* FP32 transforms/derivatives/products, FP64 state, history and solves */
+  MGB_PREC_SPLIT = 1,  /* FP32 transforms/derivatives/products, FP64 state, history and solves */
+  MGB_PREC_DFLOAT = 2  /* double-float (FP32 pair, 48-bit significand) transforms, derivatives and
+                          products on the FP32 pipes; FP64 state, history and solves */
 } mgb_precision;
 
 /* Grid and discretisation, the subset of Parameters the path depends on

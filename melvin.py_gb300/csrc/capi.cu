@@ -26,42 +26,53 @@ int cuda_check(cudaError_t e, const char* what) {
 
 static bool pow2_in_range(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; }
 
-// exp(-2*pi*i*t/n), t in [0, n), evaluated in long double; the values on the
-// axes are exact.
-static void twiddles(int n, std::vector<double>& d, std::vector<float>& f) {
-  d.resize(2 * (size_t)n);
-  f.resize(2 * (size_t)n);
+// exp(-2*pi*i*t/n), t in [0, n), evaluated in long double (the values on
+// the axes exact), then rounded to double, float and double-float.
+static void twiddle_ld(int n, std::vector<long double>& re, std::vector<long double>& im) {
+  re.resize(n);
+  im.resize(n);
   const long double pi = 3.141592653589793238462643383279502884L;
   for (int t = 0; t < n; ++t) {
     long double c, s;
-    if (t == 0) {
-      c = 1.0L, s = 0.0L;
-    } else if (4 * t == n) {
-      c = 0.0L, s = 1.0L;
-    } else if (2 * t == n) {
-      c = -1.0L, s = 0.0L;
-    } else if (4 * t == 3 * n) {
-      c = 0.0L, s = -1.0L;
-    } else {
+    if (t == 0) c = 1.0L, s = 0.0L;
+    else if (4 * t == n) c = 0.0L, s = 1.0L;
+    else if (2 * t == n) c = -1.0L, s = 0.0L;
+    else if (4 * t == 3 * n) c = 0.0L, s = -1.0L;
+    else {
       const long double ang = 2.0L * pi * (long double)t / (long double)n;
       c = cosl(ang);
       s = sinl(ang);
     }
-    d[2 * t] = (double)c;
-    d[2 * t + 1] = (double)(-s);
-    f[2 * t] = (float)c;
-    f[2 * t + 1] = (float)(-s);
+    re[t] = c;
+    im[t] = -s;
   }
 }
 
-static int upload_twiddles(int n, void** td, void** tf) {
-  std::vector<double> d;
-  std::vector<float> f;
-  twiddles(n, d, f);
+static df64 to_df64(long double v) {
+  const float h = (float)v;
+  return df64(h, (float)(v - (long double)h));
+}
+
+static int upload_twiddles(int n, void** td, void** tf, void** tdf) {
+  std::vector<long double> re, im;
+  twiddle_ld(n, re, im);
+  std::vector<double> d(2 * (size_t)n);
+  std::vector<float> f(2 * (size_t)n);
+  std::vector<df64> q(2 * (size_t)n);
+  for (int t = 0; t < n; ++t) {
+    d[2 * t] = (double)re[t];
+    d[2 * t + 1] = (double)im[t];
+    f[2 * t] = (float)re[t];
+    f[2 * t + 1] = (float)im[t];
+    q[2 * t] = to_df64(re[t]);
+    q[2 * t + 1] = to_df64(im[t]);
+  }
   MGB_CUDA(cudaMalloc(td, d.size() * sizeof(double)));
   MGB_CUDA(cudaMalloc(tf, f.size() * sizeof(float)));
+  MGB_CUDA(cudaMalloc(tdf, q.size() * sizeof(df64)));
   MGB_CUDA(cudaMemcpy(*td, d.data(), d.size() * sizeof(double), cudaMemcpyHostToDevice));
   MGB_CUDA(cudaMemcpy(*tf, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+  MGB_CUDA(cudaMemcpy(*tdf, q.data(), q.size() * sizeof(df64), cudaMemcpyHostToDevice));
   return MGB_OK;
 }
 
@@ -69,8 +80,11 @@ static void release(mgb_plan* p) {
   if (!p) return;
   cudaFree(p->tw_x_d);
   cudaFree(p->tw_x_f);
+  cudaFree(p->tw_x_df);
   cudaFree(p->tw_z_d);
   cudaFree(p->tw_z_f);
+  cudaFree(p->tw_z_df);
+  cudaFree(p->tab_df);
   cudaFree(p->th_inv);
   cudaFree(p->th_cp);
   cudaFree(p->tab_d);
@@ -117,7 +131,7 @@ int mgb_plan_create(const mgb_grid* grid, mgb_plan** out) {
     return fail(MGB_ERR_UNSUPPORTED, "nz=%d: FDM z axis needs 5 <= nz <= 1800", G.nz);
   if (G.sdo != 2 && G.sdo != 4)
     return fail(MGB_ERR_INVALID, "spatial_derivative_order=%d (2 or 4)", G.sdo);
-  if (G.precision != MGB_PREC_DOUBLE && G.precision != MGB_PREC_SPLIT)
+  if (G.precision != MGB_PREC_DOUBLE && G.precision != MGB_PREC_SPLIT && G.precision != MGB_PREC_DFLOAT)
     return fail(MGB_ERR_INVALID, "precision=%d", G.precision);
   if (!(G.lx > 0) || !(G.lz > 0)) return fail(MGB_ERR_INVALID, "box lengths must be positive");
   mgb_plan* p = new (std::nothrow) mgb_plan();
@@ -140,8 +154,8 @@ int mgb_plan_create(const mgb_grid* grid, mgb_plan** out) {
   g.d2x = -((tp * tp) / (G.lx * G.lx));
   g.d2z = -((tp * tp) / (G.lz * G.lz));
   cudaGetDevice(&p->device);
-  int st = upload_twiddles(G.nx, &p->tw_x_d, &p->tw_x_f);
-  if (!st && !G.fdm_z) st = upload_twiddles(G.nz, &p->tw_z_d, &p->tw_z_f);
+  int st = upload_twiddles(G.nx, &p->tw_x_d, &p->tw_x_f, &p->tw_x_df);
+  if (!st && !G.fdm_z) st = upload_twiddles(G.nz, &p->tw_z_d, &p->tw_z_f, &p->tw_z_df);
   if (!st && !G.fdm_z) st = fs_plan_init(p);
   if (!st && G.fdm_z) st = fd_plan_init(p);
   if (st) {
@@ -172,7 +186,7 @@ int mgb_workspace_bytes(const mgb_plan* p, int32_t family, int32_t nfields, size
   CHECK_PTR(bytes);
   const size_t diag = 152 * 4 * 3 * sizeof(double) + 256;
   if (family == 0) {
-    size_t b = p->g.fdm ? fd_verb_workspace(p) : 2 * inter_bytes(p->g, false);
+    size_t b = p->g.fdm ? fd_verb_workspace(p) : 2 * inter_bytes(p->g, MGB_PREC_DOUBLE);
     *bytes = (b > diag ? b : diag) + 256;
     return MGB_OK;
   }

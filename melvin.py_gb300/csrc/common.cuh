@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "df64.cuh"
 #include "melvin_gb300.h"
 
 namespace mgb {
@@ -45,8 +46,100 @@ __device__ __forceinline__ cx<T> mul_i(cx<T> a) {
 }
 
 template <typename To, typename From>
+struct Cvt {
+  static __device__ __forceinline__ To run(From v) { return (To)v; }
+};
+
+// Precision conversions on the integer pipes.  GB300 executes F2F
+// conversions on its narrow FP64 pipe, where they cost as much as the FP32
+// transform they feed, so the conversions at the FP64-state / reduced
+// precision boundary are done on the bit patterns instead.
+
+// double -> float, round to nearest (ties away from zero); magnitudes below
+// the smallest normal float flush to signed zero, above FLT_MAX become inf.
+// Works on the two 32-bit halves so that no step can be lowered to an FP64
+// instruction.
+__device__ __forceinline__ float d2f_bits(double d) {
+  const unsigned int hi = (unsigned int)__double2hiint(d), lo = (unsigned int)__double2loint(d);
+  const unsigned int sign = hi & 0x80000000u;
+  const unsigned int lo2 = lo + (1u << 28);
+  const unsigned int hm = (hi & 0x7fffffffu) + (lo2 < lo ? 1u : 0u);
+  const int e = (int)(hm >> 20) - 896;
+  const unsigned int m = ((hm & 0xfffffu) << 3) | (lo2 >> 29);
+  const unsigned int bits = e <= 0 ? 0u : (e >= 255 ? 0x7f800000u : (((unsigned int)e << 23) | m));
+  return __uint_as_float(bits | sign);
+}
+
+// float -> double, exact (float subnormals flush to zero).
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned int b = __float_as_uint(f);
+  const unsigned int sign = b & 0x80000000u;
+  const unsigned int e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+  unsigned int hi, lo;
+  if (e == 0) {
+    hi = 0u;
+    lo = 0u;
+  } else if (e == 255) {
+    hi = 0x7ff00000u | (m >> 3);
+    lo = m << 29;
+  } else {
+    hi = ((e + 896u) << 20) | (m >> 3);
+    lo = m << 29;
+  }
+  return __hiloint2double((int)(hi | sign), (int)lo);
+}
+
+// double -> double-float: hi = the significand truncated to 24 bits, lo = the
+// remaining 29 bits rounded to a float (48 significant bits in all).
+__device__ __forceinline__ df64 d2df_bits(double d) {
+  const unsigned int h = (unsigned int)__double2hiint(d), l = (unsigned int)__double2loint(d);
+  const unsigned int sign = h & 0x80000000u;
+  const int e = (int)((h >> 20) & 0x7ffu);
+  const int ef = e - 896;
+  if (ef <= 0) return df64(__uint_as_float(sign), 0.0f);
+  if (ef >= 255) return df64(__uint_as_float(sign | 0x7f800000u), 0.0f);
+  const unsigned int m = ((h & 0xfffffu) << 3) | (l >> 29);
+  const float hi = __uint_as_float(sign | ((unsigned int)ef << 23) | m);
+  const unsigned int rem = l & 0x1fffffffu;  // value rem * 2^(e-1075)
+  const int es = e - 1075 + 127;              // biased exponent of 2^(e-1075)
+  float lo = 0.0f;
+  if (es > 0) lo = __uint2float_rn(rem) * __uint_as_float((unsigned int)es << 23);
+  return df64(hi, sign ? -lo : lo);
+}
+
+template <>
+struct Cvt<float, double> {
+  static __device__ __forceinline__ float run(double v) { return d2f_bits(v); }
+};
+template <>
+struct Cvt<double, float> {
+  static __device__ __forceinline__ double run(float v) { return f2d_bits(v); }
+};
+template <>
+struct Cvt<df64, double> {
+  static __device__ __forceinline__ df64 run(double v) { return d2df_bits(v); }
+};
+template <>
+struct Cvt<double, df64> {
+  static __device__ __forceinline__ double run(df64 v) { return f2d_bits(v.hi) + f2d_bits(v.lo); }
+};
+
+template <typename To, typename From>
 __device__ __forceinline__ cx<To> cvt(cx<From> a) {
-  return mk((To)a.x, (To)a.y);
+  return mk(Cvt<To, From>::run(a.x), Cvt<To, From>::run(a.y));
+}
+
+// Shared-memory FFT buffers hold column c of row x at x*CS + c + x/8: one
+// pad element every 8 rows breaks the bank conflicts of the strided Stockham
+// stores (rows 8 apart would otherwise map to the same banks).
+template <int CS>
+__host__ __device__ __forceinline__ int sx(int x, int c) {
+  return x * CS + c + (x >> 3);
+}
+// Elements of a padded buffer of N rows.
+template <int CS>
+__host__ __device__ constexpr int sbuf_elems(int N) {
+  return N * CS + N / 8 + 1;
 }
 
 typedef cx<double> zd;

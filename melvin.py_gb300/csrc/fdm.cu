@@ -207,7 +207,7 @@ static FdWork fd_carve(const mgb_plan* p, int F, void* base) {
   const GridC& g = p->g;
   const bool split = p->grid.precision == MGB_PREC_SPLIT;
   const size_t S = align256((size_t)g.nn * g.nz * sizeof(zd));
-  const size_t P = align256((size_t)g.nx * g.nz * (split ? sizeof(float) : sizeof(double)));
+  const size_t P = align256((size_t)g.nx * g.nz * (split ? sizeof(float) : sizeof(double)));  // df64 is 8 bytes
   const int nctas = ((g.nz + FD_TZ - 1) / FD_TZ) * ((g.nx + FD_TX - 1) / FD_TX);
   FdWork w = {};
   char* c = (char*)base;
@@ -241,7 +241,7 @@ static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, 
                     EventTrack* et) {
   const GridC& g = p->g;
   const int F = eq->nfields;
-  const int split = p->grid.precision == MGB_PREC_SPLIT ? 1 : 0;
+  const int prec = p->grid.precision;
   const FdLaunchers* L = fd_launchers(g.nx);
   int st = thomas(p, qeval[0], -1.0, w.psi, s);
   if (st) return st;
@@ -249,13 +249,13 @@ static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, 
   FdXinvArgs xa = {};
   xa.g = g;
   xa.fdz = fd_inv(g.sdo, g.dz);
-  xa.tw = split ? p->tw_x_f : p->tw_x_d;
+  xa.tw = twiddles_for(p, false, prec);
   xa.job[0] = FdXinvJob{w.psi, w.phys[0], nullptr, 0.0, FD_UX, nullptr};
   xa.job[1] = FdXinvJob{w.psi, w.phys[1], nullptr, 0.0, FD_UZ, nullptr};
   for (int f = 0; f < F; ++f)
     xa.job[2 + f] = FdXinvJob{qeval[f], w.phys[2 + f], hist[f] + (size_t)curr * g.nn * g.nz, eq->f[f].kappa,
                               FD_COPY, nullptr};
-  st = launched(L->xinv[split](xa, 2 + F, s), "fdm step x pass");
+  st = launched(L->xinv[prec](xa, 2 + F, s), "fdm step x pass");
   if (st) return st;
   et->mark(s);
   FdPhysArgs pa = {};
@@ -271,8 +271,10 @@ static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, 
   pa.fdx = fd_inv(g.sdo, g.dx);
   pa.fdz = fd_inv(g.sdo, g.dz);
   dim3 grid((g.nz + FD_TZ - 1) / FD_TZ, (g.nx + FD_TX - 1) / FD_TX);
-  if (split)
+  if (prec == MGB_PREC_SPLIT)
     k_fd_phys<float><<<grid, NT, 0, s>>>(pa);
+  else if (prec == MGB_PREC_DFLOAT)
+    k_fd_phys<df64><<<grid, NT, 0, s>>>(pa);
   else
     k_fd_phys<double><<<grid, NT, 0, s>>>(pa);
   MGB_LAUNCH_CHECK();
@@ -301,8 +303,8 @@ static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, 
   fa.curr = curr;
   fa.dt = dt;
   fa.inv_nx = 1.0 / (double)g.nx;
-  fa.tw = split ? p->tw_x_f : p->tw_x_d;
-  st = launched(L->xfwd[split][F - 1](fa, s), "fdm step forward x pass");
+  fa.tw = twiddles_for(p, false, prec);
+  st = launched(L->xfwd[prec][F - 1](fa, s), "fdm step forward x pass");
   if (st) return st;
   et->mark(s);
   return MGB_OK;

@@ -25,7 +25,7 @@ namespace mgb {
 // Complex columns (pairs of z columns) per CTA of an FDM x pass.
 template <typename T, int N>
 struct FdTile {
-  static constexpr int E = (sizeof(T) == 8) ? 4096 : 8192;
+  static constexpr int E = 4096;
   static constexpr int P0 = E / N;
   static constexpr int CP = P0 < 1 ? 1 : (P0 > 32 ? 32 : P0);
   static constexpr int C = 2 * CP;  // z columns
@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
   const GridC& g = a.g;
   const FdXinvJob jb = a.job[blockIdx.y];
   const int z0 = blockIdx.x * C;
-  for (int e = threadIdx.x; e < N * CP; e += NT) buf[e] = mk<T>(0, 0);
+  for (int e = threadIdx.x; e < sbuf_elems<CP>(N); e += NT) buf[e] = mk<T>(0, 0);
   __syncthreads();
   for (int e = threadIdx.x; e < g.nn * CP; e += NT) {
     const int n = e / CP, j = e - n * CP;
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
       if (za < g.nz) jb.spec_out[(size_t)n * g.nz + za] = A;
       if (zb < g.nz) jb.spec_out[(size_t)n * g.nz + zb] = B;
     }
-    put_pair<T, N, CP>(buf, j, n, mk((T)A.x, (T)A.y), mk((T)B.x, (T)B.y));
+    put_pair<T, N, CP>(buf, j, n, cvt<T>(A), cvt<T>(B));
     if (jb.diff_out) {
       if (za < g.nz) jb.diff_out[(size_t)n * g.nz + za] = fd_snabla2(g, row, n, za, jb.kappa);
       if (zb < g.nz) jb.diff_out[(size_t)n * g.nz + zb] = fd_snabla2(g, row, n, zb, jb.kappa);
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
   for (int e = threadIdx.x; e < N * CP; e += NT) {
     const int x = e / CP, j = e - x * CP;
     const int za = z0 + 2 * j;
-    const cx<T> v = buf[e];
+    const cx<T> v = buf[sx<CP>(x, j)];
     if (za < g.nz) out[(size_t)x * g.nz + za] = v.x;
     if (za + 1 < g.nz) out[(size_t)x * g.nz + za + 1] = v.y;
   }
@@ -394,18 +394,18 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
 #pragma unroll
   for (int f = 0; f < F; ++f) {
     const T* J = (const T*)a.jin[f];
-    cx<T>* bf = buf + f * N * CP;
+    cx<T>* bf = buf + f * sbuf_elems<CP>(N);
     for (int e = threadIdx.x; e < N * CP; e += NT) {
       const int x = e / CP, j = e - x * CP;
       const int za = z0 + 2 * j;
       const T va = za < g.nz ? J[(size_t)x * g.nz + za] : (T)0;
       const T vb = za + 1 < g.nz ? J[(size_t)x * g.nz + za + 1] : (T)0;
-      bf[e] = mk(va, vb);
+      bf[sx<CP>(x, j)] = mk(va, vb);
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int f = 0; f < F; ++f) block_fft<T, N, CP, CP, NT, -1>(buf + f * N * CP, (const cx<T>*)a.tw);
+  for (int f = 0; f < F; ++f) block_fft<T, N, CP, CP, NT, -1>(buf + f * sbuf_elems<CP>(N), (const cx<T>*)a.tw);
   const size_t slot = (size_t)g.nn * g.nz;
   const int e_bc = g.sdo / 2;
   for (int e = threadIdx.x; e < g.nn * C; e += NT) {
@@ -416,8 +416,8 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
     if (a.mode == FD_OUT) {
       cx<T> A, B;
       get_pair<T, N, CP>(buf, j, n, A, B);
-      const cx<T> v = part ? B : A;
-      a.out[idx] = mk((double)v.x * a.inv_nx, (double)v.y * a.inv_nx);
+      const zd v = cvt<double>(part ? B : A);
+      a.out[idx] = mk(v.x * a.inv_nx, v.y * a.inv_nx);
       continue;
     }
     zd qs[F];
@@ -426,12 +426,12 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
 #pragma unroll
     for (int f = 0; f < F; ++f) {
       cx<T> A, B;
-      get_pair<T, N, CP>(buf + f * N * CP, j, n, A, B);
-      const cx<T> v = part ? B : A;
+      get_pair<T, N, CP>(buf + f * sbuf_elems<CP>(N), j, n, A, B);
+      const zd v = cvt<double>(part ? B : A);
       // f = -vec_dot_nabla + linear terms + diffusion (already in the slot)
       zd* hs = a.hist[f] + (size_t)a.curr * slot + idx;
       const zd d = *hs;
-      zd fv = mk(d.x - (double)v.x * a.inv_nx, d.y - (double)v.y * a.inv_nx);
+      zd fv = mk(d.x - v.x * a.inv_nx, d.y - v.y * a.inv_nx);
       const FdXfField& eq = a.eq[f];
       for (int t = 0; t < eq.nterms; ++t) {
         const int sidx = eq.tsrc[t];
@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
 template <typename T, int N>
 cudaError_t launch_fd_xinv(const FdXinvArgs& a, int njobs, cudaStream_t s) {
   constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
-  const size_t smem = (size_t)N * CP * sizeof(cx<T>);
+  const size_t smem = (size_t)sbuf_elems<CP>(N) * sizeof(cx<T>);
   cudaError_t e = prep_smem(k_fd_xinv<T, N>, smem);
   if (e != cudaSuccess) return e;
   dim3 grid((a.g.nz + C - 1) / C, njobs);
@@ -482,7 +482,7 @@ cudaError_t launch_fd_xinv(const FdXinvArgs& a, int njobs, cudaStream_t s) {
 template <typename T, int N, int F>
 cudaError_t launch_fd_xfwd(const FdXfArgs& a, cudaStream_t s) {
   constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
-  constexpr size_t smem = (size_t)F * N * CP * sizeof(cx<T>);
+  constexpr size_t smem = (size_t)F * sbuf_elems<CP>(N) * sizeof(cx<T>);
   if constexpr (smem > kMaxDynSmem) {
     return cudaErrorInvalidConfiguration;
   } else {
@@ -494,8 +494,8 @@ cudaError_t launch_fd_xfwd(const FdXfArgs& a, cudaStream_t s) {
 }
 
 struct FdLaunchers {
-  cudaError_t (*xinv[2])(const FdXinvArgs&, int, cudaStream_t);  // [split]
-  cudaError_t (*xfwd[2][3])(const FdXfArgs&, cudaStream_t);      // [split][F-1]
+  cudaError_t (*xinv[3])(const FdXinvArgs&, int, cudaStream_t);  // [precision]
+  cudaError_t (*xfwd[3][3])(const FdXfArgs&, cudaStream_t);      // [precision][F-1]
 };
 
 template <int N>
@@ -509,6 +509,10 @@ FdLaunchers make_fd_launchers() {
   L.xfwd[1][0] = launch_fd_xfwd<float, N, 1>;
   L.xfwd[1][1] = launch_fd_xfwd<float, N, 2>;
   L.xfwd[1][2] = launch_fd_xfwd<float, N, 3>;
+  L.xinv[2] = launch_fd_xinv<df64, N>;
+  L.xfwd[2][0] = launch_fd_xfwd<df64, N, 1>;
+  L.xfwd[2][1] = launch_fd_xfwd<df64, N, 2>;
+  L.xfwd[2][2] = launch_fd_xfwd<df64, N, 3>;
   return L;
 }
 

@@ -25,8 +25,10 @@ struct mgb_plan {
   // spectral) z axis, in double and float.
   void* tw_x_d = nullptr;
   void* tw_x_f = nullptr;
+  void* tw_x_df = nullptr;  // double-float
   void* tw_z_d = nullptr;
   void* tw_z_f = nullptr;
+  void* tw_z_df = nullptr;
   // FDM-z: Thomas factors of the per-mode Dirichlet Poisson matrices,
   // [nn][nz] each (inverse pivots and modified upper diagonals).
   double* th_inv = nullptr;
@@ -35,6 +37,7 @@ struct mgb_plan {
   // 3 x rows*cols) and tux, tuz (float, 2 x rows*cols).
   double* tab_d = nullptr;
   float* tab_f = nullptr;
+  void* tab_df = nullptr;  // tux, tuz as double-float
   int device = 0;
   mutable std::mutex mu;
   mutable PrepRecord prep;
@@ -54,9 +57,18 @@ int cuda_check(cudaError_t e, const char* what);
   } while (0)
 #define MGB_LAUNCH_CHECK() MGB_CUDA(cudaGetLastError())
 
-// Bytes of one transform intermediate (nx rows x ld cols) of complex T.
-inline size_t inter_bytes(const GridC& g, bool split) {
-  return (size_t)g.nx * (size_t)g.cols * (split ? 8 : 16);
+// Bytes of one transform intermediate (nx rows x ld cols) of complex T:
+// complex64 for the split precision, 16 bytes (complex128 or double-float
+// pairs) otherwise.
+inline size_t inter_bytes(const GridC& g, int prec) {
+  return (size_t)g.nx * (size_t)g.cols * (prec == MGB_PREC_SPLIT ? 8 : 16);
+}
+
+// Twiddle table of the x or z axis for a precision.
+inline const void* twiddles_for(const mgb_plan* p, bool zaxis, int prec) {
+  if (prec == MGB_PREC_SPLIT) return zaxis ? p->tw_z_f : p->tw_x_f;
+  if (prec == MGB_PREC_DFLOAT) return zaxis ? p->tw_z_df : p->tw_x_df;
+  return zaxis ? p->tw_z_d : p->tw_x_d;
 }
 
 // ---- fully spectral family (spectral2d.cu) ----

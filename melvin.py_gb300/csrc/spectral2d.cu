@@ -39,11 +39,14 @@ static int launched(cudaError_t e, const char* what) {
   return MGB_OK;
 }
 
-static void set_tables(const mgb_plan* p, XinvArgs& xa, bool split) {
+static void set_tables(const mgb_plan* p, XinvArgs& xa, int prec) {
   const size_t S = (size_t)p->g.rows * p->g.cols;
-  if (split) {
+  if (prec == MGB_PREC_SPLIT) {
     xa.tux = p->tab_f;
     xa.tuz = p->tab_f + S;
+  } else if (prec == MGB_PREC_DFLOAT) {
+    xa.tux = (const df64*)p->tab_df;
+    xa.tuz = (const df64*)p->tab_df + S;
   } else {
     xa.tux = p->tab_d;
     xa.tuz = p->tab_d + S;
@@ -59,7 +62,7 @@ int fs_to_physical(const mgb_plan* p, const zd* spec, double* phys, void* work, 
   xa.g = g;
   xa.ld = g.cols;
   xa.tw = p->tw_x_d;
-  set_tables(p, xa, false);
+  set_tables(p, xa, MGB_PREC_DOUBLE);
   xa.job[0] = XinvJob{spec, SRC_COPY, work, nullptr, nullptr};
   int st = launched(Lx->xinv[0](xa, 1, s), "to_physical x pass");
   if (st) return st;
@@ -102,12 +105,12 @@ int fs_vec_dot_nabla(const mgb_plan* p, const zd* q, double* q_phys, const doubl
   const FsLaunchers* Lx = fs_launchers(g.nx);
   const FsLaunchers* Lz = fs_launchers(g.nz);
   char* w0 = (char*)work;
-  char* w1 = w0 + inter_bytes(g, false);
+  char* w1 = w0 + inter_bytes(g, MGB_PREC_DOUBLE);
   XinvArgs xa = {};
   xa.g = g;
   xa.ld = g.cols;
   xa.tw = p->tw_x_d;
-  set_tables(p, xa, false);
+  set_tables(p, xa, MGB_PREC_DOUBLE);
   xa.job[0] = XinvJob{q, SRC_COPY, w0, nullptr, nullptr};
   int st = launched(Lx->xinv[0](xa, 1, s), "vec_dot_nabla x pass");
   if (st) return st;
@@ -142,12 +145,12 @@ int fs_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* ux_s, zd* uz_s, dou
   const FsLaunchers* Lx = fs_launchers(g.nx);
   const FsLaunchers* Lz = fs_launchers(g.nz);
   char* w0 = (char*)work;
-  char* w1 = w0 + inter_bytes(g, false);
+  char* w1 = w0 + inter_bytes(g, MGB_PREC_DOUBLE);
   XinvArgs xa = {};
   xa.g = g;
   xa.ld = g.cols;
   xa.tw = p->tw_x_d;
-  set_tables(p, xa, false);
+  set_tables(p, xa, MGB_PREC_DOUBLE);
   xa.job[0] = XinvJob{w, SRC_UX, w0, ux_s, psi};
   xa.job[1] = XinvJob{w, SRC_UZ, w1, uz_s, nullptr};
   int st = launched(Lx->xinv[0](xa, 2, s), "velocity x pass");
@@ -175,10 +178,9 @@ struct FsWork {
 };
 
 static FsWork fs_carve(const mgb_plan* p, int F, void* base) {
-  const bool split = p->grid.precision == MGB_PREC_SPLIT;
   const int nin = 2 + F, nout = 2 * F;
   const int ninter = nin > nout ? nin : nout;
-  const size_t ib = al256(inter_bytes(p->g, split));
+  const size_t ib = al256(inter_bytes(p->g, p->grid.precision));
   FsWork w = {};
   char* c = (char*)base;
   size_t off = 0;
@@ -254,6 +256,10 @@ int fs_plan_init(mgb_plan* p) {
       tf[S + i] = (float)tuz;
     }
   }
+  std::vector<df64> tdf(2 * S);
+  for (size_t i = 0; i < 2 * S; ++i) tdf[i] = df64(td[i]);
+  MGB_CUDA(cudaMalloc(&p->tab_df, tdf.size() * sizeof(df64)));
+  MGB_CUDA(cudaMemcpy(p->tab_df, tdf.data(), tdf.size() * sizeof(df64), cudaMemcpyHostToDevice));
   MGB_CUDA(cudaMalloc(&p->tab_d, td.size() * sizeof(double)));
   MGB_CUDA(cudaMalloc(&p->tab_f, tf.size() * sizeof(float)));
   MGB_CUDA(cudaMemcpy(p->tab_d, td.data(), td.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -278,22 +284,22 @@ int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* con
     if (!ok) return fail(MGB_ERR_INVALID, "mgb_step: call mgb_step_prepare for this equation, dt and workspace first");
   }
   et->mark(s);
-  const int split = p->grid.precision == MGB_PREC_SPLIT ? 1 : 0;
+  const int prec = p->grid.precision;
   const FsLaunchers* Lx = fs_launchers(g.nx);
   const FsLaunchers* Lz = fs_launchers(g.nz);
   FsWork w = fs_carve(p, F, work);
-  const void* twx = split ? p->tw_x_f : p->tw_x_d;
-  const void* twz = split ? p->tw_z_f : p->tw_z_d;
+  const void* twx = twiddles_for(p, false, prec);
+  const void* twz = twiddles_for(p, true, prec);
 
   XinvArgs xa = {};
   xa.g = g;
   xa.ld = g.cols;
   xa.tw = twx;
-  set_tables(p, xa, split);
+  set_tables(p, xa, prec);
   xa.job[0] = XinvJob{(const zd*)q[0], SRC_UX, w.inter[0], nullptr, nullptr};
   xa.job[1] = XinvJob{(const zd*)q[0], SRC_UZ, w.inter[1], nullptr, nullptr};
   for (int f = 0; f < F; ++f) xa.job[2 + f] = XinvJob{(const zd*)q[f], SRC_COPY, w.inter[2 + f], nullptr, nullptr};
-  int st = launched(Lx->xinv[split](xa, 2 + F, s), "step x pass");
+  int st = launched(Lx->xinv[prec](xa, 2 + F, s), "step x pass");
   if (st) return st;
   et->mark(s);
 
@@ -308,7 +314,7 @@ int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* con
   za.partial = diag ? w.partial : nullptr;
   za.fdz = fd_inv(g.sdo, g.dz);
   za.tw = twz;
-  st = launched(Lz->zz_step[split][F - 1](za, s), "step z pass");
+  st = launched(Lz->zz_step[prec][F - 1](za, s), "step z pass");
   if (st) return st;
   et->mark(s);
 
@@ -339,7 +345,7 @@ int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* con
   fa.fdx = fd_inv(g.sdo, g.dx);
   fa.inv_norm = 1.0 / ((double)g.nx * (double)g.nz);
   fa.tw = twx;
-  st = launched(Lx->xf_step[split][F - 1](fa, s), "step forward x pass");
+  st = launched(Lx->xf_step[prec][F - 1](fa, s), "step forward x pass");
   if (st) return st;
   et->mark(s);
   if (diag) return pw_finish_diag(w.partial, g.nx / 2, 1.0 / ((double)g.nx * (double)g.nz), diag, s);

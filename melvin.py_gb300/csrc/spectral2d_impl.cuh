@@ -31,10 +31,28 @@
 
 namespace mgb {
 
-// Columns per CTA of an x pass: 64 KB of complex values in shared memory.
+// Resident CTAs per SM the compiler must allow for (register budget).  The
+// FP32 and double-float kernels are latency bound (global loads, chains of
+// dependent FP32 ops), so they ask for three and two 256-thread CTAs per SM;
+// the FP64 kernels are bound by the FP64 pipe and keep the default.
+template <typename T>
+struct MinCTAs {
+  static constexpr int value = 1;
+};
+template <>
+struct MinCTAs<float> {
+  static constexpr int value = 3;
+};
+template <>
+struct MinCTAs<df64> {
+  static constexpr int value = 2;
+};
+
+// Columns per CTA of an x pass: 4096 complex values in shared memory
+// (64 KB at 16 bytes, 32 KB at 8 bytes, so more FP32 CTAs are resident).
 template <typename T, int N>
 struct XTile {
-  static constexpr int E = (sizeof(T) == 8) ? 4096 : 8192;
+  static constexpr int E = 4096;
   static constexpr int C0 = E / N;
   static constexpr int C = C0 < 1 ? 1 : (C0 > 64 ? 64 : C0);
 };
@@ -78,7 +96,7 @@ struct XinvArgs {
 };
 
 template <typename T, int N>
-__global__ void __launch_bounds__(NT) k_xinv(const XinvArgs a) {
+__global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_xinv(const XinvArgs a) {
   constexpr int C = XTile<T, N>::C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
@@ -86,7 +104,7 @@ __global__ void __launch_bounds__(NT) k_xinv(const XinvArgs a) {
   const XinvJob jb = a.job[blockIdx.y];
   const int m0 = blockIdx.x * C;
   const T* tab = (const T*)(jb.kind == SRC_UX ? a.tux : a.tuz);
-  for (int e = threadIdx.x; e < N * C; e += NT) buf[e] = mk<T>(0, 0);
+  for (int e = threadIdx.x; e < sbuf_elems<C>(N); e += NT) buf[e] = mk<T>(0, 0);
   __syncthreads();
   for (int e = threadIdx.x; e < g.rows * C; e += NT) {
     const int r = e / C, c = e - r * C, m = m0 + c;
@@ -107,14 +125,14 @@ __global__ void __launch_bounds__(NT) k_xinv(const XinvArgs a) {
       const double rl = a.rlap[idx];
       jb.psi_out[idx] = mk(-(w.x * rl), -(w.y * rl));
     }
-    buf[row_bin(r, g.nn, N) * C + c] = v;
+    buf[sx<C>(row_bin(r, g.nn, N), c)] = v;
   }
   __syncthreads();
   block_fft<T, N, C, C, NT, +1>(buf, (const cx<T>*)a.tw);
   cx<T>* out = (cx<T>*)jb.out;
   for (int e = threadIdx.x; e < N * C; e += NT) {
     const int x = e / C, c = e - x * C, m = m0 + c;
-    if (m < g.cols) out[(size_t)x * a.ld + m] = buf[e];
+    if (m < g.cols) out[(size_t)x * a.ld + m] = buf[sx<C>(x, c)];
   }
 }
 
@@ -129,16 +147,16 @@ __device__ __forceinline__ void put_pair(cx<T>* buf, int col, int m, cx<T> A, cx
   if (m == 0) {
     buf[col] = mk(A.x, B.x);
   } else {
-    buf[m * CS + col] = mk(A.x - B.y, A.y + B.x);
-    buf[(N - m) * CS + col] = mk(A.x + B.y, B.x - A.y);
+    buf[sx<CS>(m, col)] = mk(A.x - B.y, A.y + B.x);
+    buf[sx<CS>(N - m, col)] = mk(A.x + B.y, B.x - A.y);
   }
 }
 
 // Split the forward transform Z of a + i b into the half spectra of a and b.
 template <typename T, int N, int CS>
 __device__ __forceinline__ void get_pair(const cx<T>* buf, int col, int m, cx<T>& A, cx<T>& B) {
-  const cx<T> zm = buf[m * CS + col];
-  const cx<T> zn = buf[((N - m) & (N - 1)) * CS + col];
+  const cx<T> zm = buf[sx<CS>(m, col)];
+  const cx<T> zn = buf[sx<CS>((N - m) & (N - 1), col)];
   const T h = (T)0.5;
   A = mk((zm.x + zn.x) * h, (zm.y - zn.y) * h);
   B = mk((zm.y + zn.y) * h, (zn.x - zm.x) * h);
@@ -149,11 +167,11 @@ __device__ __forceinline__ void get_pair(const cx<T>* buf, int col, int m, cx<T>
 // inv = 1/(2h) (order 2) or 1/(3h) (order 4).
 template <typename T, int N, int CS>
 __device__ __forceinline__ T fd_imag(const cx<T>* buf, int col, int i, int sdo, T inv) {
-  const T p1 = buf[((i + 1) & (N - 1)) * CS + col].y;
-  const T m1 = buf[((i - 1) & (N - 1)) * CS + col].y;
+  const T p1 = buf[sx<CS>((i + 1) & (N - 1), col)].y;
+  const T m1 = buf[sx<CS>((i - 1) & (N - 1), col)].y;
   if (sdo == 2) return (p1 - m1) * inv;
-  const T p2 = buf[((i + 2) & (N - 1)) * CS + col].y;
-  const T m2 = buf[((i - 2) & (N - 1)) * CS + col].y;
+  const T p2 = buf[sx<CS>((i + 2) & (N - 1), col)].y;
+  const T m2 = buf[sx<CS>((i - 2) & (N - 1), col)].y;
   return (((T)-0.25 * p2 + (T)2 * p1) - (T)2 * m1 + (T)0.25 * m2) * inv;
 }
 
@@ -174,7 +192,7 @@ __device__ __forceinline__ void fd_imag_columns(cx<T>* buf, int sdo, T inv) {
 #pragma unroll
     for (int i = 0; i < EPT; ++i) {
       const int z = threadIdx.x + i * NT;
-      if (z < N) buf[z * CS + col].y = v[i];
+      if (z < N) buf[sx<CS>(z, col)].y = v[i];
     }
   }
   __syncthreads();
@@ -231,7 +249,7 @@ struct ZzArgs {
 };
 
 template <typename T, int N, int F>
-__global__ void __launch_bounds__(NT) k_zz_step(const ZzArgs a) {
+__global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_zz_step(const ZzArgs a) {
   constexpr int NIN = 2 + F, NOUT = 2 * F;
   constexpr int CS = NIN > NOUT ? NIN : NOUT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -240,7 +258,7 @@ __global__ void __launch_bounds__(NT) k_zz_step(const ZzArgs a) {
   const int x0 = 2 * blockIdx.x;
   const int nm = g.cols, ld = a.ld;
   const size_t r0 = (size_t)x0 * ld, r1 = r0 + ld;
-  for (int e = threadIdx.x; e < N * CS; e += NT) buf[e] = mk<T>(0, 0);
+  for (int e = threadIdx.x; e < sbuf_elems<CS>(N); e += NT) buf[e] = mk<T>(0, 0);
   __syncthreads();
   {
     const cx<T>* ux = (const cx<T>*)a.in[0];
@@ -262,7 +280,7 @@ __global__ void __launch_bounds__(NT) k_zz_step(const ZzArgs a) {
   for (int z = threadIdx.x; z < N; z += NT) {
     cx<T> w[NIN];
 #pragma unroll
-    for (int c = 0; c < NIN; ++c) w[c] = buf[z * CS + c];
+    for (int c = 0; c < NIN; ++c) w[c] = buf[sx<CS>(z, c)];
     const T ux0 = w[0].x, uz0 = w[0].y, ux1 = w[1].x, uz1 = w[1].y;
     if (a.ux_phys) {
       a.ux_phys[(size_t)x0 * N + z] = (double)ux0;
@@ -271,15 +289,16 @@ __global__ void __launch_bounds__(NT) k_zz_step(const ZzArgs a) {
       a.uz_phys[(size_t)(x0 + 1) * N + z] = (double)uz1;
     }
     if (a.partial) {
-      ke += ((double)uz0 * uz0 + (double)ux0 * ux0) + ((double)uz1 * uz1 + (double)ux1 * ux1);
-      mx = nan_max(nan_max(mx, (double)ux0), (double)ux1);
-      mz = nan_max(nan_max(mz, (double)uz0), (double)uz1);
+      const double dx0 = (double)ux0, dz0 = (double)uz0, dx1 = (double)ux1, dz1 = (double)uz1;
+      ke += (dz0 * dz0 + dx0 * dx0) + (dz1 * dz1 + dx1 * dx1);
+      mx = nan_max(nan_max(mx, dx0), dx1);
+      mz = nan_max(nan_max(mz, dz0), dz1);
     }
 #pragma unroll
     for (int f = 0; f < F; ++f) {
       const T q0 = w[2 + f].x, q1 = w[2 + f].y;
-      buf[z * CS + f] = mk(ux0 * q0, uz0 * q0);
-      buf[z * CS + F + f] = mk(ux1 * q1, uz1 * q1);
+      buf[sx<CS>(z, f)] = mk(ux0 * q0, uz0 * q0);
+      buf[sx<CS>(z, F + f)] = mk(ux1 * q1, uz1 * q1);
     }
   }
   __syncthreads();
@@ -377,7 +396,7 @@ __device__ __forceinline__ zd ab_sum(const zd* h, size_t slot, int order, int cu
 }
 
 template <typename T, int N, int F>
-__global__ void __launch_bounds__(NT) k_xf_step(const XfArgs a) {
+__global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_xf_step(const XfArgs a) {
   constexpr int C = XTile<T, N>::C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
@@ -388,15 +407,15 @@ __global__ void __launch_bounds__(NT) k_xf_step(const XfArgs a) {
   for (int f = 0; f < F; ++f) {
     const cx<T>* A = (const cx<T>*)a.ain[f];
     const cx<T>* Cc = (const cx<T>*)a.cin[f];
-    cx<T>* bf = buf + f * N * C;
+    cx<T>* bf = buf + f * sbuf_elems<C>(N);
     for (int e = threadIdx.x; e < N * C; e += NT) {
       const int x = e / C, c = e - x * C, m = m0 + c;
-      bf[e] = (m < g.cols) ? jac_x<T, N>(A, Cc, x, m, a.ld, sdo, (T)a.fdx) : mk<T>(0, 0);
+      bf[sx<C>(x, c)] = (m < g.cols) ? jac_x<T, N>(A, Cc, x, m, a.ld, sdo, (T)a.fdx) : mk<T>(0, 0);
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int f = 0; f < F; ++f) block_fft<T, N, C, C, NT, -1>(buf + f * N * C, (const cx<T>*)a.tw);
+  for (int f = 0; f < F; ++f) block_fft<T, N, C, C, NT, -1>(buf + f * sbuf_elems<C>(N), (const cx<T>*)a.tw);
 
   // -1/(nx*nz) is a power of two for the grids built, so scaling in T is exact
   const T neg_norm = (T)(-a.inv_norm);
@@ -418,7 +437,7 @@ __global__ void __launch_bounds__(NT) k_xf_step(const XfArgs a) {
     for (int f = 0; f < F; ++f) {
       const XfField& eq = a.eq[f];
       // dq[:] = -q.vec_dot_nabla(...) + linear terms
-      const cx<T> J = buf[f * N * C + k * C + c] * neg_norm;
+      const cx<T> J = buf[f * sbuf_elems<C>(N) + sx<C>(k, c)] * neg_norm;
       zd fv = cvt<double>(J);
       for (int t = 0; t < eq.nterms; ++t) {
         const int sidx = eq.tsrc[t];
@@ -468,7 +487,7 @@ __global__ void __launch_bounds__(NT) k_zinv_phys(const ZinvArgs a) {
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const int x0 = 2 * blockIdx.x;
   const size_t r0 = (size_t)x0 * a.ld, r1 = r0 + a.ld;
-  for (int e = threadIdx.x; e < N * NF; e += NT) buf[e] = mk<T>(0, 0);
+  for (int e = threadIdx.x; e < sbuf_elems<NF>(N); e += NT) buf[e] = mk<T>(0, 0);
   __syncthreads();
   for (int m = threadIdx.x; m < a.g.cols; m += NT) {
 #pragma unroll
@@ -482,7 +501,7 @@ __global__ void __launch_bounds__(NT) k_zinv_phys(const ZinvArgs a) {
   for (int z = threadIdx.x; z < N; z += NT) {
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
-      const cx<T> w = buf[z * NF + f];
+      const cx<T> w = buf[sx<NF>(z, f)];
       a.out[f][(size_t)x0 * N + z] = (double)w.x;
       a.out[f][(size_t)(x0 + 1) * N + z] = (double)w.y;
     }
@@ -503,7 +522,7 @@ __global__ void __launch_bounds__(NT) k_zfwd_phys(const ZfwdArgs a) {
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const int x0 = 2 * blockIdx.x;
   for (int z = threadIdx.x; z < N; z += NT)
-    buf[z] = mk((T)a.in[(size_t)x0 * N + z], (T)a.in[(size_t)(x0 + 1) * N + z]);
+    buf[sx<1>(z, 0)] = mk((T)a.in[(size_t)x0 * N + z], (T)a.in[(size_t)(x0 + 1) * N + z]);
   __syncthreads();
   block_fft<T, N, 1, 1, NT, -1>(buf, (const cx<T>*)a.tw);
   cx<T>* out = (cx<T>*)a.out;
@@ -537,7 +556,7 @@ __global__ void __launch_bounds__(NT) k_zz_vdn(const ZvdnArgs a) {
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const int x0 = 2 * blockIdx.x;
   const size_t r0 = (size_t)x0 * a.ld, r1 = r0 + a.ld;
-  for (int e = threadIdx.x; e < N * CS; e += NT) buf[e] = mk<T>(0, 0);
+  for (int e = threadIdx.x; e < sbuf_elems<CS>(N); e += NT) buf[e] = mk<T>(0, 0);
   __syncthreads();
   const cx<T>* q = (const cx<T>*)a.qin;
   for (int m = threadIdx.x; m < a.g.cols; m += NT) put_pair<T, N, CS>(buf, 0, m, q[r0 + m], q[r1 + m]);
@@ -545,12 +564,12 @@ __global__ void __launch_bounds__(NT) k_zz_vdn(const ZvdnArgs a) {
   block_fft<T, N, 1, CS, NT, +1>(buf, (const cx<T>*)a.tw);
   const size_t p0 = (size_t)x0 * N, p1 = p0 + N;
   for (int z = threadIdx.x; z < N; z += NT) {
-    const cx<T> w = buf[z * CS];
+    const cx<T> w = buf[sx<CS>(z, 0)];
     const double q0 = (double)w.x, q1 = (double)w.y;
     a.qphys[p0 + z] = q0;
     a.qphys[p1 + z] = q1;
-    buf[z * CS + 0] = mk((T)(a.ux[p0 + z] * q0), (T)(a.uz[p0 + z] * q0));
-    buf[z * CS + 1] = mk((T)(a.ux[p1 + z] * q1), (T)(a.uz[p1 + z] * q1));
+    buf[sx<CS>(z, 0)] = mk((T)(a.ux[p0 + z] * q0), (T)(a.uz[p0 + z] * q0));
+    buf[sx<CS>(z, 1)] = mk((T)(a.ux[p1 + z] * q1), (T)(a.uz[p1 + z] * q1));
   }
   __syncthreads();
   fd_imag_columns<T, N, CS, 2>(buf, a.g.sdo, (T)a.fdz);
@@ -592,14 +611,14 @@ __global__ void __launch_bounds__(NT) k_xf_out(const XfOutArgs a) {
     const int x = e / C, c = e - x * C, m = m0 + c;
     cx<T> v = mk<T>(0, 0);
     if (m < g.cols) v = Cc ? jac_x<T, N>(A, Cc, x, m, a.ld, g.sdo, (T)a.fdx) : A[(size_t)x * a.ld + m];
-    buf[e] = v;
+    buf[sx<C>(x, c)] = v;
   }
   __syncthreads();
   block_fft<T, N, C, C, NT, -1>(buf, (const cx<T>*)a.tw);
   for (int e = threadIdx.x; e < g.rows * C; e += NT) {
     const int r = e / C, c = e - r * C, m = m0 + c;
     if (m >= g.cols) continue;
-    const cx<T> v = buf[row_bin(r, g.nn, N) * C + c];
+    const cx<T> v = buf[sx<C>(row_bin(r, g.nn, N), c)];
     a.out[(size_t)r * g.cols + m] = mk((double)v.x * a.scale, (double)v.y * a.scale);
   }
 }
@@ -620,7 +639,7 @@ inline cudaError_t prep_smem(K kernel, size_t smem) {
 template <typename T, int N>
 cudaError_t launch_xinv(const XinvArgs& a, int njobs, cudaStream_t s) {
   constexpr int C = XTile<T, N>::C;
-  const size_t smem = (size_t)N * C * sizeof(cx<T>);
+  const size_t smem = (size_t)sbuf_elems<C>(N) * sizeof(cx<T>);
   cudaError_t e = prep_smem(k_xinv<T, N>, smem);
   if (e != cudaSuccess) return e;
   dim3 grid((a.g.cols + C - 1) / C, njobs);
@@ -635,7 +654,7 @@ constexpr size_t kMaxDynSmem = 232448 - 1024;
 template <typename T, int N, int F>
 cudaError_t launch_zz_step(const ZzArgs& a, cudaStream_t s) {
   constexpr int CS = (2 + F) > (2 * F) ? (2 + F) : (2 * F);
-  constexpr size_t smem = (size_t)N * CS * sizeof(cx<T>);
+  constexpr size_t smem = (size_t)sbuf_elems<CS>(N) * sizeof(cx<T>);
   if constexpr (smem > kMaxDynSmem) {
     return cudaErrorInvalidConfiguration;
   } else {
@@ -649,7 +668,7 @@ cudaError_t launch_zz_step(const ZzArgs& a, cudaStream_t s) {
 template <typename T, int N, int F>
 cudaError_t launch_xf_step(const XfArgs& a, cudaStream_t s) {
   constexpr int C = XTile<T, N>::C;
-  constexpr size_t smem = (size_t)F * N * C * sizeof(cx<T>);
+  constexpr size_t smem = (size_t)F * sbuf_elems<C>(N) * sizeof(cx<T>);
   if constexpr (smem > kMaxDynSmem) {
     return cudaErrorInvalidConfiguration;
   } else {
@@ -662,7 +681,7 @@ cudaError_t launch_xf_step(const XfArgs& a, cudaStream_t s) {
 
 template <int N, int NF>
 cudaError_t launch_zinv_phys(const ZinvArgs& a, cudaStream_t s) {
-  const size_t smem = (size_t)N * NF * sizeof(zd);
+  const size_t smem = (size_t)sbuf_elems<NF>(N) * sizeof(zd);
   cudaError_t e = prep_smem(k_zinv_phys<double, N, NF>, smem);
   if (e != cudaSuccess) return e;
   k_zinv_phys<double, N, NF><<<a.g.nx / 2, NT, smem, s>>>(a);
@@ -671,7 +690,7 @@ cudaError_t launch_zinv_phys(const ZinvArgs& a, cudaStream_t s) {
 
 template <int N>
 cudaError_t launch_zfwd_phys(const ZfwdArgs& a, cudaStream_t s) {
-  const size_t smem = (size_t)N * sizeof(zd);
+  const size_t smem = (size_t)sbuf_elems<1>(N) * sizeof(zd);
   cudaError_t e = prep_smem(k_zfwd_phys<double, N>, smem);
   if (e != cudaSuccess) return e;
   k_zfwd_phys<double, N><<<a.g.nx / 2, NT, smem, s>>>(a);
@@ -680,7 +699,7 @@ cudaError_t launch_zfwd_phys(const ZfwdArgs& a, cudaStream_t s) {
 
 template <int N>
 cudaError_t launch_zz_vdn(const ZvdnArgs& a, cudaStream_t s) {
-  const size_t smem = (size_t)N * 2 * sizeof(zd);
+  const size_t smem = (size_t)sbuf_elems<2>(N) * sizeof(zd);
   cudaError_t e = prep_smem(k_zz_vdn<double, N>, smem);
   if (e != cudaSuccess) return e;
   k_zz_vdn<double, N><<<a.g.nx / 2, NT, smem, s>>>(a);
@@ -690,7 +709,7 @@ cudaError_t launch_zz_vdn(const ZvdnArgs& a, cudaStream_t s) {
 template <int N>
 cudaError_t launch_xf_out(const XfOutArgs& a, cudaStream_t s) {
   constexpr int C = XTile<double, N>::C;
-  const size_t smem = (size_t)N * C * sizeof(zd);
+  const size_t smem = (size_t)sbuf_elems<C>(N) * sizeof(zd);
   cudaError_t e = prep_smem(k_xf_out<double, N>, smem);
   if (e != cudaSuccess) return e;
   k_xf_out<double, N><<<(a.g.cols + C - 1) / C, NT, smem, s>>>(a);
@@ -699,9 +718,9 @@ cudaError_t launch_xf_out(const XfOutArgs& a, cudaStream_t s) {
 
 // Table of launchers for one length N, filled by the per-N translation units.
 struct FsLaunchers {
-  cudaError_t (*xinv[2])(const XinvArgs&, int, cudaStream_t);       // [split]
-  cudaError_t (*zz_step[2][3])(const ZzArgs&, cudaStream_t);         // [split][F-1]
-  cudaError_t (*xf_step[2][3])(const XfArgs&, cudaStream_t);
+  cudaError_t (*xinv[3])(const XinvArgs&, int, cudaStream_t);       // [precision]
+  cudaError_t (*zz_step[3][3])(const ZzArgs&, cudaStream_t);         // [precision][F-1]
+  cudaError_t (*xf_step[3][3])(const XfArgs&, cudaStream_t);
   cudaError_t (*zinv_phys[2])(const ZinvArgs&, cudaStream_t);        // [NF-1]
   cudaError_t (*zfwd_phys)(const ZfwdArgs&, cudaStream_t);
   cudaError_t (*zz_vdn)(const ZvdnArgs&, cudaStream_t);
@@ -713,18 +732,25 @@ FsLaunchers make_fs_launchers() {
   FsLaunchers L;
   L.xinv[0] = launch_xinv<double, N>;
   L.xinv[1] = launch_xinv<float, N>;
+  L.xinv[2] = launch_xinv<df64, N>;
   L.zz_step[0][0] = launch_zz_step<double, N, 1>;
   L.zz_step[0][1] = launch_zz_step<double, N, 2>;
   L.zz_step[0][2] = launch_zz_step<double, N, 3>;
   L.zz_step[1][0] = launch_zz_step<float, N, 1>;
   L.zz_step[1][1] = launch_zz_step<float, N, 2>;
   L.zz_step[1][2] = launch_zz_step<float, N, 3>;
+  L.zz_step[2][0] = launch_zz_step<df64, N, 1>;
+  L.zz_step[2][1] = launch_zz_step<df64, N, 2>;
+  L.zz_step[2][2] = launch_zz_step<df64, N, 3>;
   L.xf_step[0][0] = launch_xf_step<double, N, 1>;
   L.xf_step[0][1] = launch_xf_step<double, N, 2>;
   L.xf_step[0][2] = launch_xf_step<double, N, 3>;
   L.xf_step[1][0] = launch_xf_step<float, N, 1>;
   L.xf_step[1][1] = launch_xf_step<float, N, 2>;
   L.xf_step[1][2] = launch_xf_step<float, N, 3>;
+  L.xf_step[2][0] = launch_xf_step<df64, N, 1>;
+  L.xf_step[2][1] = launch_xf_step<df64, N, 2>;
+  L.xf_step[2][2] = launch_xf_step<df64, N, 3>;
   L.zinv_phys[0] = launch_zinv_phys<N, 1>;
   L.zinv_phys[1] = launch_zinv_phys<N, 2>;
   L.zfwd_phys = launch_zfwd_phys<N>;

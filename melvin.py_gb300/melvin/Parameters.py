@@ -6,6 +6,10 @@ Same keys, defaults, validation and derived-shape rules as the reference
 * ``precision = "split"``: FP32 transforms, derivatives and products with an
   FP64 spectral state and history (``"single"`` is treated the same way, so
   state stays complex128 in every mode);
+* ``precision = "dfloat"``: transforms, derivatives and products in
+  double-float arithmetic (pairs of FP32 numbers, 48-bit significand) on the
+  FP32 pipes, with an FP64 state and history -- FP64-class accuracy at a
+  fraction of the cost of FP64 arithmetic on GB300;
 * ``device``: the CUDA device that holds every array (default ``"cuda"``).
 """
 
@@ -77,12 +81,12 @@ class Parameters:
         self.physical_shape = (self.nx, self.nz)
         self.dx = self.lx / self.nx
         self.dz = self.lz / self.nz
-        if self.precision in ("double", "split", "single"):
+        if self.precision in ("double", "split", "single", "dfloat"):
             # the prognostic state is FP64 in every precision mode
             self.complex = np.complex128
             self.float = np.float64
         else:
-            raise ValueError(f"precision={self.precision!r}: use 'double', 'split' or 'single'")
+            raise ValueError(f"precision={self.precision!r}: use 'double', 'dfloat', 'split' or 'single'")
         if "initial_dt" not in params:
             self.initial_dt = 0.2 * min(self.dx, self.dz)
 

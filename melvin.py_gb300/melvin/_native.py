@@ -24,6 +24,8 @@ MGB_ERR_NOMEM = 6
 
 PREC_DOUBLE = 0
 PREC_SPLIT = 1
+PREC_DFLOAT = 2
+PRECISIONS = {"double": PREC_DOUBLE, "split": PREC_SPLIT, "single": PREC_SPLIT, "dfloat": PREC_DFLOAT}
 
 INT_SEMI_IMPLICIT = 0
 INT_EXPLICIT = 1
@@ -231,7 +233,7 @@ def plan_for(params, device=None) -> Plan:
     fdm = params.discretisation[1] == "fdm"
     if params.discretisation[0] != "spectral":
         raise NotImplementedError("Finite difference not implemented in x direction")
-    prec = PREC_SPLIT if params.precision in ("split", "single") else PREC_DOUBLE
+    prec = PRECISIONS[params.precision]
     key = (params.nx, params.nz, float(params.lx), float(params.lz), fdm, params.spatial_derivative_order, prec, str(dev))
     p = _plans.get(key)
     if p is None:

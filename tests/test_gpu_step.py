@@ -51,10 +51,12 @@ def stepper_for(tag, sim, V, D, integ):
     raise KeyError(tag)
 
 
+@pytest.mark.parametrize("precision", ["double", "dfloat"])
 @pytest.mark.parametrize("tag", list(TRAJ_CASES))
-def test_fused_step_matches_reference_trajectory(cuda, golden, tag):
+def test_fused_step_matches_reference_trajectory(cuda, golden, tag, precision):
+    """FP64 and double-float transforms both hold the 1e-12 per-step bound."""
     g, specs, names, integ, order, dt = TRAJ_CASES[tag]
-    sim, p, V, D, bf = build(g, names, integ, order, dt)
+    sim, p, V, D, bf = build(g, names, integ, order, dt, precision)
     for n in names:
         V[n].sets(golden[f"{tag}/s0_{n}"])
     step = stepper_for(tag, sim, V, D, integ)
@@ -173,7 +175,10 @@ def test_split_precision_close_to_fp64(cuda, golden, tag):
 @pytest.mark.parametrize(
     "nx,nz,fdm,precision,integ,order,tol",
     [(2048, 2048, False, "double", "semi-implicit", 2, TOL),
+     (2048, 2048, False, "dfloat", "semi-implicit", 2, TOL),
      (2048, 2048, False, "split", "semi-implicit", 2, 1e-5),
+     (256, 4096, False, "dfloat", "semi-implicit", 2, TOL),
+     (1024, 513, True, "dfloat", "pece", 4, TOL),
      (4096, 256, False, "double", "semi-implicit", 4, TOL),
      (1024, 513, True, "double", "pece", 4, TOL),
      (1024, 513, True, "split", "pece", 4, 1e-5),
