@@ -129,6 +129,26 @@ int mgb_velocity_from_vorticity(const mgb_plan* plan, const void* w_spec, void* 
                                 void* ux_spec, void* uz_spec, double* psi_phys,
                                 double* ux_phys, double* uz_phys, void* work, void* stream);
 
+/* Size of the built-in scratch array used by mgb_vec_dot_nabla_noalloc. */
+#define MGB_NOALLOC_SCRATCH_BYTES (4u << 20)
+
+/* mgb_vec_dot_nabla for callers that cannot allocate device memory: code
+ * running under a framework that owns every device allocation and passes a
+ * kernel only its operands and results, or a section (real-time loop,
+ * stream capture) where allocation is not allowed.  Same inputs, outputs
+ * and results as mgb_vec_dot_nabla, but the transform scratch comes from a
+ * fixed MGB_NOALLOC_SCRATCH_BYTES array in the library's device memory
+ * (held by every GPU that loads the library until the process exits), so
+ * the call allocates nothing.  Grids whose scratch would exceed it (2*nx*nm
+ * complex128 fully spectral, nx*nz doubles for FDM-z; e.g. 512x512 fits)
+ * are rejected with MGB_ERR_UNSUPPORTED.  The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  All calls on a
+ * device share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  No counterpart in the reference. */
+int mgb_vec_dot_nabla_noalloc(const mgb_plan* plan, const void* q_spec, double* q_phys, const double* ux,
+                              const double* uz, void* out_spec, void* stream);
+
 /* ---- time integration (melvin/Integrator.py) --------------------------- */
 
 /* _semi_implicit_spectral (:58-63): var = ((1+(1-a)dt L) var + AB(hist)) /

@@ -109,6 +109,7 @@ SIGNATURES = {
     "mgb_laplacian": [_P, _P, _P],
     "mgb_poisson_solve": [_P, _P, _P, _P],
     "mgb_vec_dot_nabla": [_P, _P, _P, _P, _P, _P, _P, _P],
+    "mgb_vec_dot_nabla_noalloc": [_P, _P, _P, _P, _P, _P, _P],
     "mgb_velocity_from_vorticity": [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "mgb_integrate_semi_implicit": [_P, _P, _P, _I, _I, _D, _D, _P, _P],
     "mgb_integrate_explicit": [_P, _P, _P, _I, _I, _D, _P, _P],
