@@ -242,6 +242,34 @@ int mgb_step_prepare(const mgb_plan* plan, const mgb_equation* eq, double dt, vo
 int mgb_step(const mgb_plan* plan, const mgb_equation* eq, void* const* q, void* const* hist,
              int32_t curr, double dt, void* work, double* diag, void* stream);
 
+/* A batch of independent simulations on one grid, advanced together by
+ * mgb_batch_step: every kernel of the step covers all members (the last grid
+ * dimension indexes the member).  Slot k's fields sit at
+ *   states     q    + (k*nfields + f) * rows*cols            (complex128)
+ *   histories  hist + ((k*nfields + f) * order) * rows*cols  (complex128)
+ * so a pool of slots can hold simulations that start and finish at
+ * different times: `members` lists the slots to advance in this call.
+ * Extends the per-simulation loop of the examples (e.g.
+ * examples/kelvin_helmholtz_instability.py:115-131) to an ensemble. */
+typedef struct mgb_batch {
+  int32_t count;            /* members advanced by this call, 1..65535 */
+  const int32_t* members;   /* device array of `count` slot indices, or NULL for slots 0..count-1 */
+  void* q;                  /* states, complex128 [slots][nfields][rows][cols] */
+  void* hist;               /* histories, complex128 [slots][nfields][order][rows][cols] */
+  const double* term_coef;  /* optional device [slots][3][4]: per-slot coefficients of the
+                               equation's linear terms (replacing mgb_term.coef), e.g. a
+                               per-run density ratio */
+} mgb_batch;
+
+/* Scratch bytes of mgb_batch_step for `count` members. */
+int mgb_batch_workspace_bytes(const mgb_plan* plan, int32_t nfields, int32_t count, size_t* bytes);
+/* mgb_step for a batch: one call advances every listed member by one step
+ * (same equation, dt and curr for all; mgb_step_prepare on the same
+ * workspace first).  `diag` (device, count x 3 doubles, may be NULL)
+ * receives each member's kinetic energy, max ux, max uz. */
+int mgb_batch_step(const mgb_plan* plan, const mgb_equation* eq, const mgb_batch* batch, int32_t curr,
+                   double dt, void* work, double* diag, void* stream);
+
 /* Number of kernels one mgb_step launches for `eq` on this plan (not
  * counting the diagnostics fold): 3 fully spectral, 4 FDM-z explicit, 8
  * FDM-z predictor-corrector.  No reference counterpart (instrumentation). */

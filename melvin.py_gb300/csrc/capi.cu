@@ -3,6 +3,8 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <map>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -22,6 +24,22 @@ int fail(int status, const char* fmt, ...) {
 
 int cuda_check(cudaError_t e, const char* what) {
   return fail(MGB_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+// Shared-memory opt-ins already made: (kernel, device) -> largest size set.
+static std::mutex g_optin_mu;
+static std::map<std::pair<const void*, int>, size_t> g_optin;
+
+bool smem_optin_done(const void* kernel, int device, size_t smem) {
+  std::lock_guard<std::mutex> lock(g_optin_mu);
+  auto it = g_optin.find({kernel, device});
+  return it != g_optin.end() && it->second >= smem;
+}
+
+void smem_optin_record(const void* kernel, int device, size_t smem) {
+  std::lock_guard<std::mutex> lock(g_optin_mu);
+  size_t& v = g_optin[{kernel, device}];
+  if (smem > v) v = smem;
 }
 
 static bool pow2_in_range(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; }
@@ -323,6 +341,32 @@ int mgb_diagnostics(const mgb_plan* p, const double* ux, const double* uz, doubl
   return pw_diagnostics(p, ux, uz, out, work, (cudaStream_t)stream);
 }
 
+static int check_equation(const mgb_equation* eq, int32_t curr) {
+  const int F = eq->nfields;
+  if (F < 1 || F > 3) return fail(MGB_ERR_INVALID, "nfields=%d (1..3)", F);
+  if (eq->order != 2 && eq->order != 4) return fail(MGB_ERR_INVALID, "integrator_order=%d (2 or 4)", eq->order);
+  if (curr < 0 || curr >= eq->order) return fail(MGB_ERR_INVALID, "curr_idx=%d out of range", curr);
+  for (int f = 0; f < F; ++f) {
+    const mgb_field_eq& fe = eq->f[f];
+    if (fe.nterms < 0 || fe.nterms > 4) return fail(MGB_ERR_INVALID, "field %d: nterms=%d (0..4)", f, fe.nterms);
+    for (int t = 0; t < fe.nterms; ++t) {
+      if (fe.terms[t].src < -1 || fe.terms[t].src >= F)
+        return fail(MGB_ERR_INVALID, "field %d term %d: src=%d", f, t, fe.terms[t].src);
+      if (fe.terms[t].op < 0 || fe.terms[t].op > 2)
+        return fail(MGB_ERR_INVALID, "field %d term %d: op=%d", f, t, fe.terms[t].op);
+    }
+  }
+  return MGB_OK;
+}
+
+static int dispatch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb, int32_t curr, double dt,
+                         void* work, double* diag, void* stream, EventTrack* et) {
+  if (p->g.fdm) return fd_batch_step(p, eq, sb, curr, dt, work, diag, (cudaStream_t)stream, et);
+  if (eq->integrator != MGB_INT_SEMI_IMPLICIT && eq->integrator != MGB_INT_EXPLICIT)
+    return fail(MGB_ERR_UNSUPPORTED, "fully spectral step: integrator %d", eq->integrator);
+  return fs_batch_step(p, eq, sb, curr, dt, work, diag, (cudaStream_t)stream, et);
+}
+
 static int step_impl(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist, int32_t curr,
                      double dt, void* work, double* diag, void* stream, EventTrack* et) {
   CHECK_PLAN(p);
@@ -331,9 +375,8 @@ static int step_impl(const mgb_plan* p, const mgb_equation* eq, void* const* q, 
   CHECK_PTR(hist);
   CHECK_PTR(work);
   const int F = eq->nfields;
-  if (F < 1 || F > 3) return fail(MGB_ERR_INVALID, "nfields=%d (1..3)", F);
-  if (eq->order != 2 && eq->order != 4) return fail(MGB_ERR_INVALID, "integrator_order=%d (2 or 4)", eq->order);
-  if (curr < 0 || curr >= eq->order) return fail(MGB_ERR_INVALID, "curr_idx=%d out of range", curr);
+  int st = check_equation(eq, curr);
+  if (st) return st;
   for (int f = 0; f < F; ++f) {
     if (!q[f] || !hist[f]) return fail(MGB_ERR_INVALID, "null state or history for field %d", f);
     const mgb_field_eq& fe = eq->f[f];
@@ -345,15 +388,53 @@ static int step_impl(const mgb_plan* p, const mgb_equation* eq, void* const* q, 
         return fail(MGB_ERR_INVALID, "field %d term %d: op=%d", f, t, fe.terms[t].op);
     }
   }
-  if (p->g.fdm) return fd_step(p, eq, q, hist, curr, dt, work, diag, (cudaStream_t)stream, et);
-  if (eq->integrator != MGB_INT_SEMI_IMPLICIT && eq->integrator != MGB_INT_EXPLICIT)
-    return fail(MGB_ERR_UNSUPPORTED, "fully spectral step: integrator %d", eq->integrator);
-  return fs_step(p, eq, q, hist, curr, dt, work, diag, (cudaStream_t)stream, et);
+  StepBatch sb;
+  sb.count = 1;
+  for (int f = 0; f < F; ++f) {
+    sb.q[f] = (zd*)q[f];
+    sb.hist[f] = (zd*)hist[f];
+  }
+  return dispatch_step(p, eq, sb, curr, dt, work, diag, stream, et);
 }
 
 int mgb_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist, int32_t curr, double dt,
              void* work, double* diag, void* stream) {
   return step_impl(p, eq, q, hist, curr, dt, work, diag, stream, nullptr);
+}
+
+int mgb_batch_workspace_bytes(const mgb_plan* p, int32_t nfields, int32_t count, size_t* bytes) {
+  CHECK_PLAN(p);
+  CHECK_PTR(bytes);
+  if (nfields < 1 || nfields > 3) return fail(MGB_ERR_INVALID, "nfields=%d (1..3)", nfields);
+  if (count < 1) return fail(MGB_ERR_INVALID, "count=%d", count);
+  *bytes = (p->g.fdm ? fd_batch_workspace(p, nfields, count) : fs_batch_workspace(p, nfields, count)) + 256;
+  return MGB_OK;
+}
+
+int mgb_batch_step(const mgb_plan* p, const mgb_equation* eq, const mgb_batch* batch, int32_t curr, double dt,
+                   void* work, double* diag, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(eq);
+  CHECK_PTR(batch);
+  CHECK_PTR(work);
+  CHECK_PTR(batch->q);
+  CHECK_PTR(batch->hist);
+  int st = check_equation(eq, curr);
+  if (st) return st;
+  if (batch->count < 1 || batch->count > 65535) return fail(MGB_ERR_INVALID, "batch count=%d", batch->count);
+  const int F = eq->nfields;
+  const size_t S = (size_t)p->g.rows * p->g.cols;
+  StepBatch sb;
+  sb.count = batch->count;
+  sb.members = batch->members;
+  sb.q_stride = (size_t)F * S;
+  sb.h_stride = (size_t)F * eq->order * S;
+  sb.tcoef = batch->term_coef;
+  for (int f = 0; f < F; ++f) {
+    sb.q[f] = (zd*)batch->q + (size_t)f * S;
+    sb.hist[f] = (zd*)batch->hist + (size_t)f * eq->order * S;
+  }
+  return dispatch_step(p, eq, sb, curr, dt, work, diag, stream, nullptr);
 }
 
 int mgb_step_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void* work, void* stream) {

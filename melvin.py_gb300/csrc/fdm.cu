@@ -90,13 +90,14 @@ inline int grid_for(size_t n) {
   return (int)(b > 152 * 16 ? 152 * 16 : (b < 1 ? 1 : b));
 }
 
-int thomas(const mgb_plan* p, const zd* rhs, double sign, zd* out, cudaStream_t s) {
+int thomas(const mgb_plan* p, Mptr rhs, double sign, Mptr out, const int* members, int nb, cudaStream_t s) {
   const GridC& g = p->g;
   const size_t smem = (size_t)TH_MODES * g.nz * sizeof(zd);
   if (smem > kMaxDynSmem) return fail(MGB_ERR_UNSUPPORTED, "nz=%d too large for the Thomas kernel", g.nz);
   cudaError_t e = prep_smem(k_thomas, smem);
   if (e != cudaSuccess) return cuda_check(e, "thomas smem");
-  k_thomas<<<(g.nn + TH_MODES - 1) / TH_MODES, NT, smem, s>>>(g, rhs, sign, out, p->th_inv, p->th_cp);
+  k_thomas<<<dim3((g.nn + TH_MODES - 1) / TH_MODES, nb), NT, smem, s>>>(g, rhs, sign, out, members, p->th_inv,
+                                                                        p->th_cp);
   MGB_LAUNCH_CHECK();
   return MGB_OK;
 }
@@ -133,28 +134,30 @@ int fd_plan_init(mgb_plan* p) {
   return MGB_OK;
 }
 
-int fd_poisson(const mgb_plan* p, const zd* rhs, zd* out, cudaStream_t s) { return thomas(p, rhs, 1.0, out, s); }
+int fd_poisson(const mgb_plan* p, const zd* rhs, zd* out, cudaStream_t s) {
+  return thomas(p, mp(rhs), 1.0, mp(out), nullptr, 1, s);
+}
 
 int fd_to_physical(const mgb_plan* p, const zd* spec, double* phys, cudaStream_t s) {
   const GridC& g = p->g;
   FdXinvArgs xa = {};
   xa.g = g;
   xa.tw = p->tw_x_d;
-  xa.job[0] = FdXinvJob{spec, phys, nullptr, 0.0, FD_COPY, nullptr};
-  return launched(fd_launchers(g.nx)->xinv[0](xa, 1, s), "fdm to_physical");
+  xa.job[0] = FdXinvJob{mp(spec), mp(phys), mp(nullptr), 0.0, FD_COPY, nullptr};
+  return launched(fd_launchers(g.nx)->xinv[0](xa, 1, 1, s), "fdm to_physical");
 }
 
 int fd_to_spectral(const mgb_plan* p, const double* phys, zd* spec, cudaStream_t s) {
   const GridC& g = p->g;
   FdXfArgs fa = {};
   fa.g = g;
-  fa.jin[0] = phys;
+  fa.jin[0] = mp(phys);
   fa.out = spec;
   fa.nf = 1;
   fa.mode = FD_OUT;
   fa.inv_nx = 1.0 / (double)g.nx;
   fa.tw = p->tw_x_d;
-  return launched(fd_launchers(g.nx)->xfwd[0][0](fa, s), "fdm to_spectral");
+  return launched(fd_launchers(g.nx)->xfwd[0][0](fa, 1, s), "fdm to_spectral");
 }
 
 size_t fd_verb_workspace(const mgb_plan* p) {
@@ -176,31 +179,28 @@ int fd_vec_dot_nabla(const mgb_plan* p, const zd* q, double* q_phys, const doubl
 int fd_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* uz_s, double* psi_phys, double* ux, double* uz,
                 void* work, cudaStream_t s) {
   const GridC& g = p->g;
-  int st = thomas(p, w, -1.0, psi, s);
+  int st = thomas(p, mp(w), -1.0, mp(psi), nullptr, 1, s);
   if (st) return st;
   double* pp = psi_phys ? psi_phys : (double*)work;
   FdXinvArgs xa = {};
   xa.g = g;
   xa.fdz = fd_inv(g.sdo, g.dz);
   xa.tw = p->tw_x_d;
-  xa.job[0] = FdXinvJob{psi, pp, nullptr, 0.0, FD_COPY, nullptr};
-  xa.job[1] = FdXinvJob{psi, uz, nullptr, 0.0, FD_UZ, uz_s};
-  st = launched(fd_launchers(g.nx)->xinv[0](xa, 2, s), "fdm velocity x pass");
+  xa.job[0] = FdXinvJob{mp(psi), mp(pp), mp(nullptr), 0.0, FD_COPY, nullptr};
+  xa.job[1] = FdXinvJob{mp(psi), mp(uz), mp(nullptr), 0.0, FD_UZ, uz_s};
+  st = launched(fd_launchers(g.nx)->xinv[0](xa, 2, 1, s), "fdm velocity x pass");
   if (st) return st;
   k_fd_vel<<<grid_for((size_t)g.nx * g.nz), NT, 0, s>>>(g, pp, ux, fd_inv(g.sdo, g.dz));
   MGB_LAUNCH_CHECK();
   return MGB_OK;
 }
 
-// Scratch of the fused FDM step: psi_hat, physical psi and fields, J per
-// field, predicted states (PECE), diagnostics partials.
+// Scratch of the fused FDM step, per member: psi_hat, physical ux, uz and
+// fields, J per field, predicted states (PECE), diagnostics partials.
 struct FdWork {
-  zd* psi;
-  void* phys[5];
-  void* J[3];
-  zd* qpred[3];
-  double* partial;
-  size_t bytes;
+  size_t psi, phys[5], J[3], qpred[3], partial;  // byte offsets in a member block
+  size_t member_bytes;
+  char* base;
 };
 
 static FdWork fd_carve(const mgb_plan* p, int F, void* base) {
@@ -210,67 +210,81 @@ static FdWork fd_carve(const mgb_plan* p, int F, void* base) {
   const size_t P = align256((size_t)g.nx * g.nz * (split ? sizeof(float) : sizeof(double)));  // df64 is 8 bytes
   const int nctas = ((g.nz + FD_TZ - 1) / FD_TZ) * ((g.nx + FD_TX - 1) / FD_TX);
   FdWork w = {};
-  char* c = (char*)base;
   size_t off = 0;
-  w.psi = (zd*)(c + off);
+  w.psi = off;
   off += S;
   for (int i = 0; i < 2 + F; ++i) {
-    w.phys[i] = c + off;
+    w.phys[i] = off;
     off += P;
   }
   for (int f = 0; f < F; ++f) {
-    w.J[f] = c + off;
+    w.J[f] = off;
     off += P;
   }
   for (int f = 0; f < F; ++f) {
-    w.qpred[f] = (zd*)(c + off);
+    w.qpred[f] = off;
     off += S;
   }
-  w.partial = (double*)(c + off);
+  w.partial = off;
   off += align256((size_t)nctas * 3 * sizeof(double));
-  w.bytes = off;
+  w.member_bytes = off;
+  w.base = (char*)base;
   return w;
 }
 
-size_t fd_step_workspace(const mgb_plan* p, int nfields) { return fd_carve(p, nfields, nullptr).bytes; }
+static inline Mptr wmp(const FdWork& w, size_t off) { return mp(w.base + off, w.member_bytes, 0); }
 
-// One evaluation of the right-hand side at states `qeval` followed by the
-// update selected by `mode`.
-static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, zd* const* q, zd* const* qeval,
-                    zd* const* hist, int curr, double dt, int mode, double* diag_partial, cudaStream_t s,
-                    EventTrack* et) {
+size_t fd_step_workspace(const mgb_plan* p, int nfields) { return fd_carve(p, nfields, nullptr).member_bytes; }
+size_t fd_batch_workspace(const mgb_plan* p, int nfields, int count) {
+  return fd_carve(p, nfields, nullptr).member_bytes * (size_t)count;
+}
+
+// One evaluation of the right-hand side at the states `qeval` (the members'
+// own states, or their predicted states in scratch) followed by the update
+// selected by `mode`.
+static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, const StepBatch& sb, bool eval_pred,
+                    int curr, double dt, int mode, bool diag, cudaStream_t s, EventTrack* et) {
   const GridC& g = p->g;
   const int F = eq->nfields;
+  const int nb = sb.count;
   const int prec = p->grid.precision;
   const FdLaunchers* L = fd_launchers(g.nx);
-  int st = thomas(p, qeval[0], -1.0, w.psi, s);
+  const size_t qs = sb.q_stride * sizeof(zd), hs = sb.h_stride * sizeof(zd);
+  Mptr qev[3], qown[3], hist[3], hslot[3];
+  for (int f = 0; f < F; ++f) {
+    qown[f] = mp(sb.q[f], qs, 1);
+    qev[f] = eval_pred ? wmp(w, w.qpred[f]) : qown[f];
+    hist[f] = mp(sb.hist[f], hs, 1);
+    hslot[f] = mp(sb.hist[f] + (size_t)curr * g.nn * g.nz, hs, 1);
+  }
+  int st = thomas(p, qev[0], -1.0, wmp(w, w.psi), sb.members, nb, s);
   if (st) return st;
   et->mark(s);
   FdXinvArgs xa = {};
   xa.g = g;
   xa.fdz = fd_inv(g.sdo, g.dz);
   xa.tw = twiddles_for(p, false, prec);
-  xa.job[0] = FdXinvJob{w.psi, w.phys[0], nullptr, 0.0, FD_UX, nullptr};
-  xa.job[1] = FdXinvJob{w.psi, w.phys[1], nullptr, 0.0, FD_UZ, nullptr};
+  xa.members = sb.members;
+  xa.job[0] = FdXinvJob{wmp(w, w.psi), wmp(w, w.phys[0]), mp(nullptr), 0.0, FD_UX, nullptr};
+  xa.job[1] = FdXinvJob{wmp(w, w.psi), wmp(w, w.phys[1]), mp(nullptr), 0.0, FD_UZ, nullptr};
   for (int f = 0; f < F; ++f)
-    xa.job[2 + f] = FdXinvJob{qeval[f], w.phys[2 + f], hist[f] + (size_t)curr * g.nn * g.nz, eq->f[f].kappa,
-                              FD_COPY, nullptr};
-  st = launched(L->xinv[prec](xa, 2 + F, s), "fdm step x pass");
+    xa.job[2 + f] = FdXinvJob{qev[f], wmp(w, w.phys[2 + f]), hslot[f], eq->f[f].kappa, FD_COPY, nullptr};
+  st = launched(L->xinv[prec](xa, 2 + F, nb, s), "fdm step x pass");
   if (st) return st;
   et->mark(s);
   FdPhysArgs pa = {};
   pa.g = g;
-  pa.ux = w.phys[0];
-  pa.uz = w.phys[1];
+  pa.ux = wmp(w, w.phys[0]);
+  pa.uz = wmp(w, w.phys[1]);
   for (int f = 0; f < F; ++f) {
-    pa.q[f] = w.phys[2 + f];
-    pa.jout[f] = w.J[f];
+    pa.q[f] = wmp(w, w.phys[2 + f]);
+    pa.jout[f] = wmp(w, w.J[f]);
   }
   pa.nf = F;
-  pa.partial = diag_partial;
+  pa.partial = diag ? wmp(w, w.partial) : mp(nullptr);
   pa.fdx = fd_inv(g.sdo, g.dx);
   pa.fdz = fd_inv(g.sdo, g.dz);
-  dim3 grid((g.nz + FD_TZ - 1) / FD_TZ, (g.nx + FD_TX - 1) / FD_TX);
+  dim3 grid((g.nz + FD_TZ - 1) / FD_TZ, (g.nx + FD_TX - 1) / FD_TX, nb);
   if (prec == MGB_PREC_SPLIT)
     k_fd_phys<float><<<grid, NT, 0, s>>>(pa);
   else if (prec == MGB_PREC_DFLOAT)
@@ -281,11 +295,13 @@ static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, 
   et->mark(s);
   FdXfArgs fa = {};
   fa.g = g;
+  fa.members = sb.members;
+  fa.tcoef = sb.tcoef;
   for (int f = 0; f < F; ++f) {
-    fa.jin[f] = w.J[f];
-    fa.q[f] = q[f];
-    fa.qsrc[f] = qeval[f];
-    fa.qpred[f] = w.qpred[f];
+    fa.jin[f] = wmp(w, w.J[f]);
+    fa.q[f] = qown[f];
+    fa.qsrc[f] = qev[f];
+    fa.qpred[f] = wmp(w, w.qpred[f]);
     fa.hist[f] = hist[f];
     const mgb_field_eq& fe = eq->f[f];
     fa.eq[f].nterms = fe.nterms;
@@ -296,7 +312,7 @@ static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, 
       fa.eq[f].tcoef[t] = fe.terms[t].coef;
     }
   }
-  fa.psi = w.psi;
+  fa.psi = wmp(w, w.psi);
   fa.nf = F;
   fa.mode = mode;
   fa.order = eq->order;
@@ -304,14 +320,14 @@ static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, 
   fa.dt = dt;
   fa.inv_nx = 1.0 / (double)g.nx;
   fa.tw = twiddles_for(p, false, prec);
-  st = launched(L->xfwd[prec][F - 1](fa, s), "fdm step forward x pass");
+  st = launched(L->xfwd[prec][F - 1](fa, nb, s), "fdm step forward x pass");
   if (st) return st;
   et->mark(s);
   return MGB_OK;
 }
 
-int fd_step(const mgb_plan* p, const mgb_equation* eq, void* const* qv, void* const* hv, int curr, double dt,
-            void* work, double* diag, cudaStream_t s, EventTrack* et) {
+int fd_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb, int curr, double dt, void* work,
+                  double* diag, cudaStream_t s, EventTrack* et) {
   EventTrack none;
   if (!et) et = &none;
   et->mark(s);
@@ -322,31 +338,31 @@ int fd_step(const mgb_plan* p, const mgb_equation* eq, void* const* qv, void* co
       if (eq->f[f].terms[t].op == 2)
         return fail(MGB_ERR_UNSUPPORTED, "d/dz linear terms are not pointwise on an FDM z axis");
   FdWork w = fd_carve(p, F, work);
-  zd* q[3] = {nullptr, nullptr, nullptr};
-  zd* h[3] = {nullptr, nullptr, nullptr};
-  for (int f = 0; f < F; ++f) {
-    q[f] = (zd*)qv[f];
-    h[f] = (zd*)hv[f];
-  }
   const int nctas = ((g.nz + FD_TZ - 1) / FD_TZ) * ((g.nx + FD_TX - 1) / FD_TX);
-  double* part = diag ? w.partial : nullptr;
   int st;
   if (eq->integrator == MGB_INT_EXPLICIT) {
-    st = fd_stage(p, eq, w, q, q, h, curr, dt, FD_EXPLICIT, part, s, et);
+    st = fd_stage(p, eq, w, sb, false, curr, dt, FD_EXPLICIT, diag != nullptr, s, et);
   } else if (eq->integrator == MGB_INT_PECE) {
-    // predict into w.qpred, then evaluate there and correct q in place; the
-    // corrector's f* goes to the next slot, which the caller's advance makes
-    // the next step's f0 slot.
-    st = fd_stage(p, eq, w, q, q, h, curr, dt, FD_PREDICT, part, s, et);
+    // predict into scratch, then evaluate there and correct the states in
+    // place; the corrector's f* goes to the next slot, which the caller's
+    // advance makes the next step's f0 slot.
+    st = fd_stage(p, eq, w, sb, false, curr, dt, FD_PREDICT, diag != nullptr, s, et);
     if (st) return st;
     const int next = (curr + 1) % eq->order;
-    st = fd_stage(p, eq, w, q, w.qpred, h, next, dt, FD_CORRECT, nullptr, s, et);
+    st = fd_stage(p, eq, w, sb, true, next, dt, FD_CORRECT, false, s, et);
   } else {
     return fail(MGB_ERR_UNSUPPORTED,
                 "semi-implicit integration needs a fully spectral grid (melvin/Integrator.py:78-81)");
   }
   if (st) return st;
-  if (diag) return pw_finish_diag(w.partial, nctas, 1.0 / ((double)g.nx * (double)g.nz), diag, s);
+  if (diag) {
+    // per-member partials sit member_bytes apart: fold each member's block
+    for (int z = 0; z < sb.count; ++z) {
+      st = pw_finish_diag((const double*)(w.base + (size_t)z * w.member_bytes + w.partial), nctas, 1,
+                          1.0 / ((double)g.nx * (double)g.nz), diag + 3 * z, s);
+      if (st) return st;
+    }
+  }
   return MGB_OK;
 }
 

@@ -31,6 +31,20 @@ struct FdTile {
   static constexpr int C = 2 * CP;  // z columns
 };
 
+// Address of a per-member array in a batched launch: member z uses
+// base + k * stride bytes, with k the member's slot (arrays owned by the
+// caller, e.g. states and histories) or z itself (step scratch).
+struct Mptr {
+  void* base;
+  size_t stride;  // bytes
+  int by_slot;
+};
+__device__ __forceinline__ char* maddr(const Mptr& p, const int* members, int z) {
+  const int k = (p.by_slot && members) ? members[z] : z;
+  return (char*)p.base + (size_t)k * p.stride;
+}
+inline Mptr mp(const void* base, size_t stride = 0, int by_slot = 0) { return Mptr{(void*)base, stride, by_slot}; }
+
 // pd2dz2 of a complex spectral row at z (interior only), times kappa, plus
 // kappa * d2x n^2 q  ==  kappa * snabla2(q) (melvin/Variable.py:111-113).
 __device__ __forceinline__ zd fd_snabla2(const GridC& g, const zd* row, int n, int z, double kappa) {
@@ -62,11 +76,14 @@ __device__ __forceinline__ zd fd_snabla2(const GridC& g, const zd* row, int n, i
 
 constexpr int TH_MODES = 8;  // modes per CTA
 
-static __global__ void __launch_bounds__(NT) k_thomas(GridC g, const zd* __restrict__ rhs, double rhs_sign,
-                                               zd* __restrict__ out, const double* __restrict__ inv_piv,
+// Member = blockIdx.y.
+static __global__ void __launch_bounds__(NT) k_thomas(GridC g, Mptr rhs_p, double rhs_sign, Mptr out_p,
+                                               const int* members, const double* __restrict__ inv_piv,
                                                const double* __restrict__ cp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   zd* rows = reinterpret_cast<zd*>(smem_raw);  // [TH_MODES][nz]
+  const zd* rhs = (const zd*)maddr(rhs_p, members, blockIdx.y);
+  zd* out = (zd*)maddr(out_p, members, blockIdx.y);
   const int n0 = blockIdx.x * TH_MODES;
   const int nz = g.nz;
   const int nm = min(TH_MODES, g.nn - n0);
@@ -113,12 +130,12 @@ enum FdKind : int {
 };
 
 struct FdXinvJob {
-  const zd* src;
-  void* phys;     // T [nx][nz]
-  zd* diff_out;   // optional: kappa * snabla2(src) -> history slot
+  Mptr src;       // zd [nn][nz]
+  Mptr phys;      // T [nx][nz]
+  Mptr diff_out;  // optional (base null): kappa * snabla2(src) -> history slot
   double kappa;
   int kind;       // FdKind
-  zd* spec_out;   // optional: the transformed spectral field (uz spectral data)
+  zd* spec_out;   // optional, single member: the transformed spectral field (uz spectral data)
 };
 
 // First-derivative z stencil of a complex spectral row (Dirichlet: the
@@ -138,6 +155,7 @@ struct FdXinvArgs {
   FdXinvJob job[5];
   double fdz;    // 1/(2dz) or 1/(3dz)
   const void* tw;
+  const int* members;  // member = blockIdx.z
 };
 
 template <typename T, int N>
@@ -148,12 +166,14 @@ __global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
   const GridC& g = a.g;
   const FdXinvJob jb = a.job[blockIdx.y];
   const int z0 = blockIdx.x * C;
+  const zd* src = (const zd*)maddr(jb.src, a.members, blockIdx.z);
+  zd* dout = jb.diff_out.base ? (zd*)maddr(jb.diff_out, a.members, blockIdx.z) : nullptr;
   for (int e = threadIdx.x; e < sbuf_elems<CP>(N); e += NT) buf[e] = mk<T>(0, 0);
   __syncthreads();
   for (int e = threadIdx.x; e < g.nn * CP; e += NT) {
     const int n = e / CP, j = e - n * CP;
     const int za = z0 + 2 * j, zb = za + 1;
-    const zd* row = jb.src + (size_t)n * g.nz;
+    const zd* row = src + (size_t)n * g.nz;
     zd A = mk(0.0, 0.0), B = mk(0.0, 0.0);
     if (jb.kind == FD_UX) {
       if (za < g.nz) A = fd_ddz_row(row, za, g.nz, g.sdo, a.fdz);
@@ -174,14 +194,14 @@ __global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
       if (zb < g.nz) jb.spec_out[(size_t)n * g.nz + zb] = B;
     }
     put_pair<T, N, CP>(buf, j, n, cvt<T>(A), cvt<T>(B));
-    if (jb.diff_out) {
-      if (za < g.nz) jb.diff_out[(size_t)n * g.nz + za] = fd_snabla2(g, row, n, za, jb.kappa);
-      if (zb < g.nz) jb.diff_out[(size_t)n * g.nz + zb] = fd_snabla2(g, row, n, zb, jb.kappa);
+    if (dout) {
+      if (za < g.nz) dout[(size_t)n * g.nz + za] = fd_snabla2(g, row, n, za, jb.kappa);
+      if (zb < g.nz) dout[(size_t)n * g.nz + zb] = fd_snabla2(g, row, n, zb, jb.kappa);
     }
   }
   __syncthreads();
   block_fft<T, N, CP, CP, NT, +1>(buf, (const cx<T>*)a.tw);
-  T* out = (T*)jb.phys;
+  T* out = (T*)maddr(jb.phys, a.members, blockIdx.z);
   for (int e = threadIdx.x; e < N * CP; e += NT) {
     const int x = e / CP, j = e - x * CP;
     const int za = z0 + 2 * j;
@@ -199,11 +219,11 @@ constexpr int FD_TX = 16, FD_TZ = 64;
 
 struct FdPhysArgs {
   GridC g;
-  const void* ux;    // T [nx][nz]
-  const void* uz;    // T [nx][nz]
-  const void* q[3];  // T [nx][nz]
-  void* jout[3];     // T [nx][nz]
-  double* partial;   // optional per-CTA diagnostics (sum ux^2+uz^2, max ux, max uz)
+  Mptr ux;           // T [nx][nz], per member
+  Mptr uz;
+  Mptr q[3];
+  Mptr jout[3];
+  Mptr partial;      // optional (base null): per-CTA diagnostics (sum ux^2+uz^2, max ux, max uz)
   int nf;
   double fdx, fdz;   // 1/(2dx) or 1/(3dx); same for z
 };
@@ -227,8 +247,8 @@ __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
   const int nx = g.nx, nz = g.nz, sdo = g.sdo, h = sdo / 2;
   const int x0 = blockIdx.y * FD_TX, z0 = blockIdx.x * FD_TZ;
   const T fdx = (T)a.fdx, fdz = (T)a.fdz;
-  const T* ux = (const T*)a.ux;
-  const T* uz = (const T*)a.uz;
+  const T* ux = (const T*)maddr(a.ux, nullptr, blockIdx.z);
+  const T* uz = (const T*)maddr(a.uz, nullptr, blockIdx.z);
   for (int e = threadIdx.x; e < SX * FD_TZ; e += NT) {
     const int i = e / FD_TZ, k = e - i * FD_TZ;
     const int x = (x0 + i - H + nx) % nx, z = z0 + k;
@@ -241,7 +261,7 @@ __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
   }
   __syncthreads();
   double ke = 0, mx = -INFINITY, mz = -INFINITY;
-  if (a.partial) {
+  if (a.partial.base) {
     for (int e = threadIdx.x; e < FD_TX * FD_TZ; e += NT) {
       const int i = e / FD_TZ, k = e - i * FD_TZ;
       if (x0 + i < nx && z0 + k < nz) {
@@ -253,14 +273,14 @@ __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
     }
   }
   for (int f = 0; f < a.nf; ++f) {
-    const T* q = (const T*)a.q[f];
+    const T* q = (const T*)maddr(a.q[f], nullptr, blockIdx.z);
     for (int e = threadIdx.x; e < SX * SZ; e += NT) {
       const int i = e / SZ, k = e - i * SZ;
       const int x = (x0 + i - H + nx) % nx, z = z0 + k - H;
       s_q[i][k] = (z >= 0 && z < nz) ? q[(size_t)x * nz + z] : (T)0;
     }
     __syncthreads();
-    T* jo = (T*)a.jout[f];
+    T* jo = (T*)maddr(a.jout[f], nullptr, blockIdx.z);
     for (int e = threadIdx.x; e < FD_TX * FD_TZ; e += NT) {
       const int i = e / FD_TZ, k = e - i * FD_TZ;
       const int x = x0 + i, z = z0 + k;
@@ -276,7 +296,7 @@ __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
     }
     __syncthreads();
   }
-  if (a.partial) {
+  if (a.partial.base) {
     __shared__ double red[3][NT / 32];
     for (int o = 16; o > 0; o >>= 1) {
       ke += __shfl_xor_sync(0xffffffffu, ke, o);
@@ -298,9 +318,10 @@ __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
         MZ = (red[2][i] != red[2][i] || red[2][i] > MZ) ? red[2][i] : MZ;
       }
       const int cta = blockIdx.y * gridDim.x + blockIdx.x;
-      a.partial[3 * cta + 0] = S;
-      a.partial[3 * cta + 1] = MX;
-      a.partial[3 * cta + 2] = MZ;
+      double* part = (double*)maddr(a.partial, nullptr, blockIdx.z);
+      part[3 * cta + 0] = S;
+      part[3 * cta + 1] = MX;
+      part[3 * cta + 2] = MZ;
     }
   }
 }
@@ -326,13 +347,15 @@ struct FdXfField {
 
 struct FdXfArgs {
   GridC g;
-  const void* jin[3];  // T [nx][nz]
-  zd* q[3];            // states: read (all modes); written for EXPLICIT / CORRECT
-  const zd* qsrc[3];   // states the linear terms read (q, or the predicted state)
-  zd* qpred[3];        // PREDICT output
-  zd* hist[3];
-  const zd* psi;       // spectral psi of the evaluated state (for src = -1 terms)
-  zd* out;             // FD_OUT target
+  Mptr jin[3];         // T [nx][nz]
+  Mptr q[3];           // states: read (all modes); written for EXPLICIT / CORRECT
+  Mptr qsrc[3];        // states the linear terms read (q, or the predicted state)
+  Mptr qpred[3];       // PREDICT output
+  Mptr hist[3];
+  Mptr psi;            // spectral psi of the evaluated state (for src = -1 terms)
+  zd* out;             // FD_OUT target (single member)
+  const int* members;  // member = blockIdx.y
+  const double* tcoef; // optional per-slot term coefficients [slot][3][4]
   int nf, mode, order, curr;
   double dt, inv_nx;
   FdXfField eq[3];
@@ -391,9 +414,11 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const GridC& g = a.g;
   const int z0 = blockIdx.x * C;
+  const int zm = blockIdx.y;
+  const int slot = a.members ? a.members[zm] : zm;
 #pragma unroll
   for (int f = 0; f < F; ++f) {
-    const T* J = (const T*)a.jin[f];
+    const T* J = (const T*)maddr(a.jin[f], a.members, zm);
     cx<T>* bf = buf + f * sbuf_elems<CP>(N);
     for (int e = threadIdx.x; e < N * CP; e += NT) {
       const int x = e / CP, j = e - x * CP;
@@ -406,8 +431,21 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
   __syncthreads();
 #pragma unroll
   for (int f = 0; f < F; ++f) block_fft<T, N, CP, CP, NT, -1>(buf + f * sbuf_elems<CP>(N), (const cx<T>*)a.tw);
-  const size_t slot = (size_t)g.nn * g.nz;
+  const size_t hslot = (size_t)g.nn * g.nz;
   const int e_bc = g.sdo / 2;
+  zd* qf[F];
+  const zd* qs_[F];
+  zd* qp[F];
+  zd* hf[F];
+#pragma unroll
+  for (int f = 0; f < F; ++f) {
+    qf[f] = (zd*)maddr(a.q[f], a.members, zm);
+    qs_[f] = (const zd*)maddr(a.qsrc[f], a.members, zm);
+    qp[f] = a.qpred[f].base ? (zd*)maddr(a.qpred[f], a.members, zm) : nullptr;
+    hf[f] = (zd*)maddr(a.hist[f], a.members, zm);
+  }
+  const zd* psi = a.psi.base ? (const zd*)maddr(a.psi, a.members, zm) : nullptr;
+  const double* tco = a.tcoef ? a.tcoef + (size_t)slot * 12 : nullptr;
   for (int e = threadIdx.x; e < g.nn * C; e += NT) {
     const int n = e / C, c = e - n * C, z = z0 + c;
     if (z >= g.nz) continue;
@@ -422,20 +460,20 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
     }
     zd qs[F];
 #pragma unroll
-    for (int f = 0; f < F; ++f) qs[f] = a.qsrc[f][idx];
+    for (int f = 0; f < F; ++f) qs[f] = qs_[f][idx];
 #pragma unroll
     for (int f = 0; f < F; ++f) {
       cx<T> A, B;
       get_pair<T, N, CP>(buf + f * sbuf_elems<CP>(N), j, n, A, B);
       const zd v = cvt<double>(part ? B : A);
       // f = -vec_dot_nabla + linear terms + diffusion (already in the slot)
-      zd* hs = a.hist[f] + (size_t)a.curr * slot + idx;
+      zd* hs = hf[f] + (size_t)a.curr * hslot + idx;
       const zd d = *hs;
       zd fv = mk(d.x - v.x * a.inv_nx, d.y - v.y * a.inv_nx);
       const FdXfField& eq = a.eq[f];
       for (int t = 0; t < eq.nterms; ++t) {
         const int sidx = eq.tsrc[t];
-        zd s = sidx < 0 ? a.psi[idx] : qs[0];
+        zd s = sidx < 0 ? psi[idx] : qs[0];
 #pragma unroll
         for (int q2 = 1; q2 < F; ++q2)
           if (sidx == q2) s = qs[q2];
@@ -443,23 +481,24 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
           const double b = g.dfx * (double)n;
           s = mk(-(b * s.y), b * s.x);
         }
-        fv = mk(fv.x + eq.tcoef[t] * s.x, fv.y + eq.tcoef[t] * s.y);
+        const double cc = tco ? tco[f * 4 + t] : eq.tcoef[t];
+        fv = mk(fv.x + cc * s.x, fv.y + cc * s.y);
       }
       *hs = fv;
-      const zd q0 = a.q[f][idx];
+      const zd q0 = qf[f][idx];
       zd qn;
       if (a.mode == FD_CORRECT) {
-        const zd am = fd_am(a.hist[f] + idx, slot, a.order, a.curr, fv, a.dt);
+        const zd am = fd_am(hf[f] + idx, hslot, a.order, a.curr, fv, a.dt);
         qn = mk(q0.x + am.x, q0.y + am.y);
       } else {
-        const zd ab = fd_ab(a.hist[f] + idx, slot, a.order, a.curr, fv, a.dt);
+        const zd ab = fd_ab(hf[f] + idx, hslot, a.order, a.curr, fv, a.dt);
         qn = mk(q0.x + ab.x, q0.y + ab.y);
       }
       qn = fd_bc(qn, eq.bc, n, z, g.nz, e_bc);
       if (a.mode == FD_PREDICT)
-        a.qpred[f][idx] = qn;
+        qp[f][idx] = qn;
       else
-        a.q[f][idx] = qn;
+        qf[f][idx] = qn;
     }
   }
 }
@@ -469,18 +508,18 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
 // ---------------------------------------------------------------------------
 
 template <typename T, int N>
-cudaError_t launch_fd_xinv(const FdXinvArgs& a, int njobs, cudaStream_t s) {
+cudaError_t launch_fd_xinv(const FdXinvArgs& a, int njobs, int nb, cudaStream_t s) {
   constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
   const size_t smem = (size_t)sbuf_elems<CP>(N) * sizeof(cx<T>);
   cudaError_t e = prep_smem(k_fd_xinv<T, N>, smem);
   if (e != cudaSuccess) return e;
-  dim3 grid((a.g.nz + C - 1) / C, njobs);
+  dim3 grid((a.g.nz + C - 1) / C, njobs, nb);
   k_fd_xinv<T, N><<<grid, NT, smem, s>>>(a);
   return cudaGetLastError();
 }
 
 template <typename T, int N, int F>
-cudaError_t launch_fd_xfwd(const FdXfArgs& a, cudaStream_t s) {
+cudaError_t launch_fd_xfwd(const FdXfArgs& a, int nb, cudaStream_t s) {
   constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
   constexpr size_t smem = (size_t)F * sbuf_elems<CP>(N) * sizeof(cx<T>);
   if constexpr (smem > kMaxDynSmem) {
@@ -488,14 +527,14 @@ cudaError_t launch_fd_xfwd(const FdXfArgs& a, cudaStream_t s) {
   } else {
     cudaError_t e = prep_smem(k_fd_xfwd<T, N, F>, smem);
     if (e != cudaSuccess) return e;
-    k_fd_xfwd<T, N, F><<<(a.g.nz + C - 1) / C, NT, smem, s>>>(a);
+    k_fd_xfwd<T, N, F><<<dim3((a.g.nz + C - 1) / C, nb), NT, smem, s>>>(a);
     return cudaGetLastError();
   }
 }
 
 struct FdLaunchers {
-  cudaError_t (*xinv[3])(const FdXinvArgs&, int, cudaStream_t);  // [precision]
-  cudaError_t (*xfwd[3][3])(const FdXfArgs&, cudaStream_t);      // [precision][F-1]
+  cudaError_t (*xinv[3])(const FdXinvArgs&, int, int, cudaStream_t);  // [precision](args, jobs, members)
+  cudaError_t (*xfwd[3][3])(const FdXfArgs&, int, cudaStream_t);      // [precision][F-1](args, members)
 };
 
 template <int N>

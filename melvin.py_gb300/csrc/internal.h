@@ -90,9 +90,22 @@ struct EventTrack {
   }
 };
 
-int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist,
-            int curr, double dt, void* work, double* diag, cudaStream_t s, EventTrack* et = nullptr);
+// Members of a batched fused step: field f of slot k has its state at
+// q[f] + k * q_stride and its history at hist[f] + k * h_stride (elements).
+// A single simulation is count = 1, members = null, zero strides.
+struct StepBatch {
+  int count = 1;
+  const int* members = nullptr;  // device slot list or null (slots 0..count-1)
+  zd* q[3] = {nullptr, nullptr, nullptr};
+  zd* hist[3] = {nullptr, nullptr, nullptr};
+  size_t q_stride = 0, h_stride = 0;
+  const double* tcoef = nullptr;  // optional device [slot][3][4] term coefficients
+};
+
+int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb, int curr, double dt, void* work,
+                  double* diag, cudaStream_t s, EventTrack* et = nullptr);
 size_t fs_step_workspace(const mgb_plan* p, int nfields);
+size_t fs_batch_workspace(const mgb_plan* p, int nfields, int count);
 int fs_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void* work, cudaStream_t s);
 int fs_plan_init(mgb_plan* p);
 
@@ -104,9 +117,10 @@ int fd_vec_dot_nabla(const mgb_plan* p, const zd* q, double* q_phys, const doubl
                      const double* uz, zd* out, void* work, cudaStream_t s);
 int fd_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* uz_s, double* psi_phys, double* ux,
                 double* uz, void* work, cudaStream_t s);
-int fd_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist,
-            int curr, double dt, void* work, double* diag, cudaStream_t s, EventTrack* et = nullptr);
+int fd_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb, int curr, double dt, void* work,
+                  double* diag, cudaStream_t s, EventTrack* et = nullptr);
 size_t fd_step_workspace(const mgb_plan* p, int nfields);
+size_t fd_batch_workspace(const mgb_plan* p, int nfields, int count);
 size_t fd_verb_workspace(const mgb_plan* p);
 int fd_plan_init(mgb_plan* p);
 
@@ -124,7 +138,8 @@ int pw_adams(const mgb_plan* p, int corrector, const zd* hist, int order, int cu
              zd* out, cudaStream_t s);
 int pw_diagnostics(const mgb_plan* p, const double* ux, const double* uz, double* out, void* work,
                    cudaStream_t s);
-// Fold per-CTA partials [n][3] (sum, max, max) into out[3] = {0.5*sum/(nx*nz), max, max}.
-int pw_finish_diag(const double* partial, int n, double inv_npts, double* out, cudaStream_t s);
+// Fold per-CTA partials [count][n][3] (sum, max, max) into
+// out[count][3] = {0.5*sum/(nx*nz), max, max}.
+int pw_finish_diag(const double* partial, int n, int count, double inv_npts, double* out, cudaStream_t s);
 
 }  // namespace mgb

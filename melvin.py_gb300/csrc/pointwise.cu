@@ -272,6 +272,8 @@ __global__ void k_diag_partial(size_t total, const double* __restrict__ ux, cons
 }
 
 __global__ void k_diag_finish(const double* __restrict__ partial, int n, double inv_npts, double* __restrict__ out) {
+  partial += (size_t)blockIdx.x * n * 3;
+  out += (size_t)blockIdx.x * 3;
   double s = 0, mx = -INFINITY, mz = -INFINITY;
   for (int i = threadIdx.x; i < n; i += PT) {
     s += partial[3 * i];
@@ -352,8 +354,8 @@ int pw_adams(const mgb_plan* p, int corrector, const zd* hist, int order, int cu
   return MGB_OK;
 }
 
-int pw_finish_diag(const double* partial, int n, double inv_npts, double* out, cudaStream_t s) {
-  k_diag_finish<<<1, PT, 0, s>>>(partial, n, inv_npts, out);
+int pw_finish_diag(const double* partial, int n, int count, double inv_npts, double* out, cudaStream_t s) {
+  k_diag_finish<<<count, PT, 0, s>>>(partial, n, inv_npts, out);
   MGB_LAUNCH_CHECK();
   return MGB_OK;
 }
@@ -366,7 +368,7 @@ int pw_diagnostics(const mgb_plan* p, const double* ux, const double* uz, double
   double* partial = (double*)work;
   k_diag_partial<<<nb, PT, 0, s>>>(total, ux, uz, partial);
   MGB_LAUNCH_CHECK();
-  return pw_finish_diag(partial, nb, 1.0 / (double)total, out, s);
+  return pw_finish_diag(partial, nb, 1, 1.0 / (double)total, out, s);
 }
 
 }  // namespace mgb

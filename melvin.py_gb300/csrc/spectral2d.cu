@@ -64,7 +64,7 @@ int fs_to_physical(const mgb_plan* p, const zd* spec, double* phys, void* work, 
   xa.tw = p->tw_x_d;
   set_tables(p, xa, MGB_PREC_DOUBLE);
   xa.job[0] = XinvJob{spec, SRC_COPY, work, nullptr, nullptr};
-  int st = launched(Lx->xinv[0](xa, 1, s), "to_physical x pass");
+  int st = launched(Lx->xinv[0](xa, 1, 1, s), "to_physical x pass");
   if (st) return st;
   ZinvArgs za = {};
   za.g = g;
@@ -112,7 +112,7 @@ int fs_vec_dot_nabla(const mgb_plan* p, const zd* q, double* q_phys, const doubl
   xa.tw = p->tw_x_d;
   set_tables(p, xa, MGB_PREC_DOUBLE);
   xa.job[0] = XinvJob{q, SRC_COPY, w0, nullptr, nullptr};
-  int st = launched(Lx->xinv[0](xa, 1, s), "vec_dot_nabla x pass");
+  int st = launched(Lx->xinv[0](xa, 1, 1, s), "vec_dot_nabla x pass");
   if (st) return st;
   ZvdnArgs za = {};
   za.g = g;
@@ -153,7 +153,7 @@ int fs_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* ux_s, zd* uz_s, dou
   set_tables(p, xa, MGB_PREC_DOUBLE);
   xa.job[0] = XinvJob{w, SRC_UX, w0, ux_s, psi};
   xa.job[1] = XinvJob{w, SRC_UZ, w1, uz_s, nullptr};
-  int st = launched(Lx->xinv[0](xa, 2, s), "velocity x pass");
+  int st = launched(Lx->xinv[0](xa, 2, 1, s), "velocity x pass");
   if (st) return st;
   ZinvArgs za = {};
   za.g = g;
@@ -168,35 +168,41 @@ int fs_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* ux_s, zd* uz_s, dou
 
 static inline size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// Step scratch: transform intermediates, diagnostics partials, per-field
-// update coefficients (a, b) per mode.
+// Step scratch: per-field update coefficients (a, b) per mode (shared by
+// all members, at a fixed offset), then per member the diagnostics partials
+// and the transform intermediates.
 struct FsWork {
-  char* inter[6];
-  double* partial;
   zd* coef[3];
+  double* partial;        // [count][nx/2][3]
+  char* inter[6];         // member 0's intermediates
+  size_t inter_stride;    // bytes between members' intermediate blocks
   size_t bytes;
 };
 
-static FsWork fs_carve(const mgb_plan* p, int F, void* base) {
+static FsWork fs_carve(const mgb_plan* p, int F, int count, void* base) {
   const int nin = 2 + F, nout = 2 * F;
   const int ninter = nin > nout ? nin : nout;
   const size_t ib = al256(inter_bytes(p->g, p->grid.precision));
   FsWork w = {};
   char* c = (char*)base;
   size_t off = 0;
-  for (int i = 0; i < 6; ++i) w.inter[i] = c + (size_t)(i < ninter ? i : ninter - 1) * ib;
-  off = (size_t)ninter * ib;
-  w.partial = (double*)(c + off);
-  off += al256((size_t)(p->g.nx / 2) * 3 * sizeof(double));
   for (int f = 0; f < 3; ++f) {
     w.coef[f] = (zd*)(c + off);
     if (f < F) off += al256((size_t)p->g.rows * p->g.cols * sizeof(zd));
   }
+  w.partial = (double*)(c + off);
+  off += al256((size_t)count * (p->g.nx / 2) * 3 * sizeof(double));
+  for (int i = 0; i < 6; ++i) w.inter[i] = c + off + (size_t)(i < ninter ? i : ninter - 1) * ib;
+  w.inter_stride = (size_t)ninter * ib;
+  off += (size_t)count * w.inter_stride;
   w.bytes = off;
   return w;
 }
 
-size_t fs_step_workspace(const mgb_plan* p, int nfields) { return fs_carve(p, nfields, nullptr).bytes; }
+size_t fs_step_workspace(const mgb_plan* p, int nfields) { return fs_carve(p, nfields, 1, nullptr).bytes; }
+size_t fs_batch_workspace(const mgb_plan* p, int nfields, int count) {
+  return fs_carve(p, nfields, count, nullptr).bytes;
+}
 
 // Per-mode update coefficients of one field, with L = kappa * lap(n, m):
 //   semi-implicit (melvin/Integrator.py:58-63):
@@ -222,7 +228,7 @@ __global__ void k_update_coefs(GridC g, double kappa, int semi, double dt, doubl
 
 int fs_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void* work, cudaStream_t s) {
   const GridC& g = p->g;
-  FsWork w = fs_carve(p, eq->nfields, work);
+  FsWork w = fs_carve(p, eq->nfields, 1, work);
   const double cab = eq->order == 2 ? dt / 2 : dt / 24;
   const size_t total = (size_t)g.rows * g.cols;
   size_t nb = (total + NT - 1) / NT;
@@ -268,12 +274,13 @@ int fs_plan_init(mgb_plan* p) {
 }
 
 
-int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist, int curr,
-            double dt, void* work, double* diag, cudaStream_t s, EventTrack* et) {
+int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb, int curr, double dt, void* work,
+                  double* diag, cudaStream_t s, EventTrack* et) {
   EventTrack none;
   if (!et) et = &none;
   const GridC& g = p->g;
   const int F = eq->nfields;
+  const int nb = sb.count;
   {
     // the update coefficients in `work` must be the ones for (eq, dt)
     std::lock_guard<std::mutex> lock(p->mu);
@@ -287,25 +294,33 @@ int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* con
   const int prec = p->grid.precision;
   const FsLaunchers* Lx = fs_launchers(g.nx);
   const FsLaunchers* Lz = fs_launchers(g.nz);
-  FsWork w = fs_carve(p, F, work);
+  FsWork w = fs_carve(p, F, nb, work);
   const void* twx = twiddles_for(p, false, prec);
   const void* twz = twiddles_for(p, true, prec);
+  BatchC bc = {};
+  bc.members = sb.members;
+  bc.q_stride = sb.q_stride;
+  bc.h_stride = sb.h_stride;
+  bc.inter_stride = w.inter_stride;
+  bc.tcoef = sb.tcoef;
 
   XinvArgs xa = {};
   xa.g = g;
   xa.ld = g.cols;
   xa.tw = twx;
+  xa.b = bc;
   set_tables(p, xa, prec);
-  xa.job[0] = XinvJob{(const zd*)q[0], SRC_UX, w.inter[0], nullptr, nullptr};
-  xa.job[1] = XinvJob{(const zd*)q[0], SRC_UZ, w.inter[1], nullptr, nullptr};
-  for (int f = 0; f < F; ++f) xa.job[2 + f] = XinvJob{(const zd*)q[f], SRC_COPY, w.inter[2 + f], nullptr, nullptr};
-  int st = launched(Lx->xinv[prec](xa, 2 + F, s), "step x pass");
+  xa.job[0] = XinvJob{sb.q[0], SRC_UX, w.inter[0], nullptr, nullptr};
+  xa.job[1] = XinvJob{sb.q[0], SRC_UZ, w.inter[1], nullptr, nullptr};
+  for (int f = 0; f < F; ++f) xa.job[2 + f] = XinvJob{sb.q[f], SRC_COPY, w.inter[2 + f], nullptr, nullptr};
+  int st = launched(Lx->xinv[prec](xa, 2 + F, nb, s), "step x pass");
   if (st) return st;
   et->mark(s);
 
   ZzArgs za = {};
   za.g = g;
   za.ld = g.cols;
+  za.b = bc;
   for (int i = 0; i < 2 + F; ++i) za.in[i] = w.inter[i];
   for (int f = 0; f < F; ++f) {
     za.aout[f] = w.inter[f];
@@ -314,20 +329,21 @@ int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* con
   za.partial = diag ? w.partial : nullptr;
   za.fdz = fd_inv(g.sdo, g.dz);
   za.tw = twz;
-  st = launched(Lz->zz_step[prec][F - 1](za, s), "step z pass");
+  st = launched(Lz->zz_step[prec][F - 1](za, nb, s), "step z pass");
   if (st) return st;
   et->mark(s);
 
   XfArgs fa = {};
   fa.g = g;
   fa.ld = g.cols;
+  fa.b = bc;
   fa.need_psi = 0;
   fa.rlap = p->tab_d + 2 * (size_t)g.rows * g.cols;
   for (int f = 0; f < F; ++f) {
     fa.ain[f] = w.inter[f];
     fa.cin[f] = w.inter[F + f];
-    fa.q[f] = (zd*)q[f];
-    fa.hist[f] = (zd*)hist[f];
+    fa.q[f] = sb.q[f];
+    fa.hist[f] = sb.hist[f];
     fa.coef[f] = w.coef[f];
     const mgb_field_eq& fe = eq->f[f];
     fa.eq[f].nterms = fe.nterms;
@@ -345,10 +361,10 @@ int fs_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* con
   fa.fdx = fd_inv(g.sdo, g.dx);
   fa.inv_norm = 1.0 / ((double)g.nx * (double)g.nz);
   fa.tw = twx;
-  st = launched(Lx->xf_step[prec][F - 1](fa, s), "step forward x pass");
+  st = launched(Lx->xf_step[prec][F - 1](fa, nb, s), "step forward x pass");
   if (st) return st;
   et->mark(s);
-  if (diag) return pw_finish_diag(w.partial, g.nx / 2, 1.0 / ((double)g.nx * (double)g.nz), diag, s);
+  if (diag) return pw_finish_diag(w.partial, g.nx / 2, nb, 1.0 / ((double)g.nx * (double)g.nz), diag, s);
   return MGB_OK;
 }
 

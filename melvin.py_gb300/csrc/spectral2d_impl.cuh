@@ -57,6 +57,20 @@ struct XTile {
   static constexpr int C = C0 < 1 ? 1 : (C0 > 64 ? 64 : C0);
 };
 
+// Batched launches: member z of a launch (the last grid dimension) works on
+// slot = members ? members[z] : z; the arrays of a slot sit at
+// base + slot * stride.  A single simulation is a batch of one with zero
+// strides.
+struct BatchC {
+  const int* members;    // device slot list, or null for slots 0..count-1
+  size_t q_stride;       // zd elements between slots of a state array
+  size_t h_stride;       // zd elements between slots of a history array
+  size_t inter_stride;   // bytes between members' intermediate blocks
+  const double* tcoef;   // optional per-slot term coefficients [slot][3][4]
+};
+
+__device__ __forceinline__ int batch_slot(const BatchC& b, int z) { return b.members ? b.members[z] : z; }
+
 template <typename T>
 __device__ __forceinline__ T nan_max(T m, T v) {
   return (v != v || v > m) ? v : m;
@@ -93,6 +107,7 @@ struct XinvArgs {
   const void* tuz;     // T[rows*cols]
   const double* rlap;  // double[rows*cols]
   const void* tw;
+  BatchC b;            // member = blockIdx.z
 };
 
 template <typename T, int N>
@@ -104,13 +119,14 @@ __global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_xinv(const XinvArgs a
   const XinvJob jb = a.job[blockIdx.y];
   const int m0 = blockIdx.x * C;
   const T* tab = (const T*)(jb.kind == SRC_UX ? a.tux : a.tuz);
+  const zd* src = jb.src + (size_t)batch_slot(a.b, blockIdx.z) * a.b.q_stride;
   for (int e = threadIdx.x; e < sbuf_elems<C>(N); e += NT) buf[e] = mk<T>(0, 0);
   __syncthreads();
   for (int e = threadIdx.x; e < g.rows * C; e += NT) {
     const int r = e / C, c = e - r * C, m = m0 + c;
     if (m >= g.cols) continue;
     const size_t idx = (size_t)r * g.cols + m;
-    const zd w = jb.src[idx];
+    const zd w = src[idx];
     const cx<T> wt = cvt<T>(w);
     cx<T> v = wt;
     if (jb.kind == SRC_UX) {
@@ -129,7 +145,7 @@ __global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_xinv(const XinvArgs a
   }
   __syncthreads();
   block_fft<T, N, C, C, NT, +1>(buf, (const cx<T>*)a.tw);
-  cx<T>* out = (cx<T>*)jb.out;
+  cx<T>* out = (cx<T>*)((char*)jb.out + (size_t)blockIdx.z * a.b.inter_stride);
   for (int e = threadIdx.x; e < N * C; e += NT) {
     const int x = e / C, c = e - x * C, m = m0 + c;
     if (m < g.cols) out[(size_t)x * a.ld + m] = buf[sx<C>(x, c)];
@@ -243,9 +259,10 @@ struct ZzArgs {
   void* cout[3];
   double* ux_phys;    // optional physical velocity
   double* uz_phys;
-  double* partial;    // optional [gridDim.x][3]
+  double* partial;    // optional [member][gridDim.x][3]
   double fdz;         // 1/(2dz) or 1/(3dz)
   const void* tw;
+  BatchC b;           // member = blockIdx.y
 };
 
 template <typename T, int N, int F>
@@ -257,18 +274,19 @@ __global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_zz_step(const ZzArgs 
   const GridC& g = a.g;
   const int x0 = 2 * blockIdx.x;
   const int nm = g.cols, ld = a.ld;
+  const size_t moff = (size_t)blockIdx.y * a.b.inter_stride;
   const size_t r0 = (size_t)x0 * ld, r1 = r0 + ld;
   for (int e = threadIdx.x; e < sbuf_elems<CS>(N); e += NT) buf[e] = mk<T>(0, 0);
   __syncthreads();
   {
-    const cx<T>* ux = (const cx<T>*)a.in[0];
-    const cx<T>* uz = (const cx<T>*)a.in[1];
+    const cx<T>* ux = (const cx<T>*)((const char*)a.in[0] + moff);
+    const cx<T>* uz = (const cx<T>*)((const char*)a.in[1] + moff);
     for (int m = threadIdx.x; m < nm; m += NT) {
       put_pair<T, N, CS>(buf, 0, m, ux[r0 + m], uz[r0 + m]);
       put_pair<T, N, CS>(buf, 1, m, ux[r1 + m], uz[r1 + m]);
 #pragma unroll
       for (int f = 0; f < F; ++f) {
-        const cx<T>* q = (const cx<T>*)a.in[2 + f];
+        const cx<T>* q = (const cx<T>*)((const char*)a.in[2 + f] + moff);
         put_pair<T, N, CS>(buf, 2 + f, m, q[r0 + m], q[r1 + m]);
       }
     }
@@ -307,8 +325,8 @@ __global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_zz_step(const ZzArgs 
   for (int m = threadIdx.x; m < nm; m += NT) {
 #pragma unroll
     for (int f = 0; f < F; ++f) {
-      cx<T>* ao = (cx<T>*)a.aout[f];
-      cx<T>* co = (cx<T>*)a.cout[f];
+      cx<T>* ao = (cx<T>*)((char*)a.aout[f] + moff);
+      cx<T>* co = (cx<T>*)((char*)a.cout[f] + moff);
 #pragma unroll
       for (int rho = 0; rho < 2; ++rho) {
         cx<T> A, Cc;
@@ -318,7 +336,7 @@ __global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_zz_step(const ZzArgs 
       }
     }
   }
-  if (a.partial) block_diag(ke, mx, mz, a.partial);
+  if (a.partial) block_diag(ke, mx, mz, a.partial + (size_t)blockIdx.y * gridDim.x * 3);
 }
 
 // ---------------------------------------------------------------------------
@@ -349,6 +367,7 @@ struct XfArgs {
   double fdx, inv_norm;
   XfField eq[3];
   const void* tw;
+  BatchC b;            // member = blockIdx.y
 };
 
 // J at (x, m): periodic x stencil of A plus C (both intermediates).
@@ -403,10 +422,12 @@ __global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_xf_step(const XfArgs 
   const GridC& g = a.g;
   const int m0 = blockIdx.x * C;
   const int sdo = g.sdo;
+  const size_t moff = (size_t)blockIdx.y * a.b.inter_stride;
+  const int mslot = batch_slot(a.b, blockIdx.y);
 #pragma unroll
   for (int f = 0; f < F; ++f) {
-    const cx<T>* A = (const cx<T>*)a.ain[f];
-    const cx<T>* Cc = (const cx<T>*)a.cin[f];
+    const cx<T>* A = (const cx<T>*)((const char*)a.ain[f] + moff);
+    const cx<T>* Cc = (const cx<T>*)((const char*)a.cin[f] + moff);
     cx<T>* bf = buf + f * sbuf_elems<C>(N);
     for (int e = threadIdx.x; e < N * C; e += NT) {
       const int x = e / C, c = e - x * C, m = m0 + c;
@@ -420,6 +441,14 @@ __global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_xf_step(const XfArgs 
   // -1/(nx*nz) is a power of two for the grids built, so scaling in T is exact
   const T neg_norm = (T)(-a.inv_norm);
   const size_t slot = (size_t)g.rows * g.cols;
+  zd* qf[F];
+  zd* hf[F];
+#pragma unroll
+  for (int f = 0; f < F; ++f) {
+    qf[f] = a.q[f] + (size_t)mslot * a.b.q_stride;
+    hf[f] = a.hist[f] + (size_t)mslot * a.b.h_stride;
+  }
+  const double* tco = a.b.tcoef ? a.b.tcoef + (size_t)mslot * 12 : nullptr;
   for (int e = threadIdx.x; e < g.rows * C; e += NT) {
     const int r = e / C, c = e - r * C, m = m0 + c;
     if (m >= g.cols) continue;
@@ -427,7 +456,7 @@ __global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_xf_step(const XfArgs 
     const size_t idx = (size_t)r * g.cols + m;
     zd qo[F];
 #pragma unroll
-    for (int f = 0; f < F; ++f) qo[f] = a.q[f][idx];
+    for (int f = 0; f < F; ++f) qo[f] = qf[f][idx];
     zd psi = mk(0.0, 0.0);
     if (a.need_psi) {
       const double rl = a.rlap[idx];
@@ -446,24 +475,25 @@ __global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_xf_step(const XfArgs 
         for (int q2 = 0; q2 < F; ++q2)
           if (sidx == q2) s = qo[q2];
         const zd v = lin_term(g, s, eq.top[t], n, m);
-        fv = mk(fv.x + eq.tcoef[t] * v.x, fv.y + eq.tcoef[t] * v.y);
+        const double cc = tco ? tco[f * 4 + t] : eq.tcoef[t];
+        fv = mk(fv.x + cc * v.x, fv.y + cc * v.y);
       }
       const zd cf = a.coef[f][idx];
       zd qn;
       if (a.integrator == MGB_INT_SEMI_IMPLICIT) {
         // q' = ((1 + (1-a) dt L) q + AB) / (1 - a dt L) = cf.x q + cf.y * sum
-        a.hist[f][(size_t)a.curr * slot + idx] = fv;
-        const zd sm = ab_sum(a.hist[f] + idx, slot, a.order, a.curr, fv);
+        hf[f][(size_t)a.curr * slot + idx] = fv;
+        const zd sm = ab_sum(hf[f] + idx, slot, a.order, a.curr, fv);
         qn = mk(cf.x * qo[f].x + cf.y * sm.x, cf.x * qo[f].y + cf.y * sm.y);
       } else {
         // explicit: the history keeps N + D, D = kappa * snabla2(q) = cf.x q
         fv = mk(fv.x + cf.x * qo[f].x, fv.y + cf.x * qo[f].y);
-        a.hist[f][(size_t)a.curr * slot + idx] = fv;
-        const zd sm = ab_sum(a.hist[f] + idx, slot, a.order, a.curr, fv);
+        hf[f][(size_t)a.curr * slot + idx] = fv;
+        const zd sm = ab_sum(hf[f] + idx, slot, a.order, a.curr, fv);
         qn = mk(qo[f].x + cf.y * sm.x, qo[f].y + cf.y * sm.y);
       }
       if ((eq.bc & MGB_BC_ZERO_M0) && m == 0) qn = mk(0.0, 0.0);
-      a.q[f][idx] = qn;
+      qf[f][idx] = qn;
     }
   }
 }
@@ -627,22 +657,33 @@ __global__ void __launch_bounds__(NT) k_xf_out(const XfOutArgs a) {
 // Launchers (one instantiation set per transform length N).
 // ---------------------------------------------------------------------------
 
-// Opt in to more than the default 48 KB of shared memory per CTA.  Kernels
-// here use at most 1 KB of static shared memory, so any dynamic request
-// above 47 KB opts in.
+// Opt in to more than the default 48 KB of shared memory per CTA, once per
+// kernel and device (the first launch sets the attribute, so later launches,
+// including those inside a stream capture, make no attribute call).  Kernels
+// here use at most 1 KB of static shared memory, so any dynamic request above
+// 47 KB opts in; the attribute is set to the largest size any launch needs.
+bool smem_optin_done(const void* kernel, int device, size_t smem);
+void smem_optin_record(const void* kernel, int device, size_t smem);
+
 template <typename K>
 inline cudaError_t prep_smem(K kernel, size_t smem) {
-  if (smem > 47 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  return cudaSuccess;
+  if (smem <= 47 * 1024) return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (smem_optin_done((const void*)kernel, dev, smem)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) smem_optin_record((const void*)kernel, dev, smem);
+  return e;
 }
 
 template <typename T, int N>
-cudaError_t launch_xinv(const XinvArgs& a, int njobs, cudaStream_t s) {
+cudaError_t launch_xinv(const XinvArgs& a, int njobs, int nb, cudaStream_t s) {
   constexpr int C = XTile<T, N>::C;
   const size_t smem = (size_t)sbuf_elems<C>(N) * sizeof(cx<T>);
   cudaError_t e = prep_smem(k_xinv<T, N>, smem);
   if (e != cudaSuccess) return e;
-  dim3 grid((a.g.cols + C - 1) / C, njobs);
+  dim3 grid((a.g.cols + C - 1) / C, njobs, nb);
   k_xinv<T, N><<<grid, NT, smem, s>>>(a);
   return cudaGetLastError();
 }
@@ -652,7 +693,7 @@ cudaError_t launch_xinv(const XinvArgs& a, int njobs, cudaStream_t s) {
 constexpr size_t kMaxDynSmem = 232448 - 1024;
 
 template <typename T, int N, int F>
-cudaError_t launch_zz_step(const ZzArgs& a, cudaStream_t s) {
+cudaError_t launch_zz_step(const ZzArgs& a, int nb, cudaStream_t s) {
   constexpr int CS = (2 + F) > (2 * F) ? (2 + F) : (2 * F);
   constexpr size_t smem = (size_t)sbuf_elems<CS>(N) * sizeof(cx<T>);
   if constexpr (smem > kMaxDynSmem) {
@@ -660,13 +701,13 @@ cudaError_t launch_zz_step(const ZzArgs& a, cudaStream_t s) {
   } else {
     cudaError_t e = prep_smem(k_zz_step<T, N, F>, smem);
     if (e != cudaSuccess) return e;
-    k_zz_step<T, N, F><<<a.g.nx / 2, NT, smem, s>>>(a);
+    k_zz_step<T, N, F><<<dim3(a.g.nx / 2, nb), NT, smem, s>>>(a);
     return cudaGetLastError();
   }
 }
 
 template <typename T, int N, int F>
-cudaError_t launch_xf_step(const XfArgs& a, cudaStream_t s) {
+cudaError_t launch_xf_step(const XfArgs& a, int nb, cudaStream_t s) {
   constexpr int C = XTile<T, N>::C;
   constexpr size_t smem = (size_t)F * sbuf_elems<C>(N) * sizeof(cx<T>);
   if constexpr (smem > kMaxDynSmem) {
@@ -674,7 +715,7 @@ cudaError_t launch_xf_step(const XfArgs& a, cudaStream_t s) {
   } else {
     cudaError_t e = prep_smem(k_xf_step<T, N, F>, smem);
     if (e != cudaSuccess) return e;
-    k_xf_step<T, N, F><<<(a.g.cols + C - 1) / C, NT, smem, s>>>(a);
+    k_xf_step<T, N, F><<<dim3((a.g.cols + C - 1) / C, nb), NT, smem, s>>>(a);
     return cudaGetLastError();
   }
 }
@@ -718,9 +759,9 @@ cudaError_t launch_xf_out(const XfOutArgs& a, cudaStream_t s) {
 
 // Table of launchers for one length N, filled by the per-N translation units.
 struct FsLaunchers {
-  cudaError_t (*xinv[3])(const XinvArgs&, int, cudaStream_t);       // [precision]
-  cudaError_t (*zz_step[3][3])(const ZzArgs&, cudaStream_t);         // [precision][F-1]
-  cudaError_t (*xf_step[3][3])(const XfArgs&, cudaStream_t);
+  cudaError_t (*xinv[3])(const XinvArgs&, int, int, cudaStream_t);  // [precision](args, jobs, members)
+  cudaError_t (*zz_step[3][3])(const ZzArgs&, int, cudaStream_t);    // [precision][F-1](args, members)
+  cudaError_t (*xf_step[3][3])(const XfArgs&, int, cudaStream_t);
   cudaError_t (*zinv_phys[2])(const ZinvArgs&, cudaStream_t);        // [NF-1]
   cudaError_t (*zfwd_phys)(const ZfwdArgs&, cudaStream_t);
   cudaError_t (*zz_vdn)(const ZvdnArgs&, cudaStream_t);

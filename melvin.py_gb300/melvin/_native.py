@@ -79,6 +79,16 @@ class MgbFieldEq(C.Structure):
     ]
 
 
+class MgbBatch(C.Structure):
+    _fields_ = [
+        ("count", C.c_int32),
+        ("members", C.c_void_p),
+        ("q", C.c_void_p),
+        ("hist", C.c_void_p),
+        ("term_coef", C.c_void_p),
+    ]
+
+
 class MgbEquation(C.Structure):
     _fields_ = [
         ("nfields", C.c_int32),
@@ -117,6 +127,8 @@ SIGNATURES = {
     "mgb_diagnostics": [_P, _P, _P, _P, _P, _P],
     "mgb_step": [_P, C.POINTER(MgbEquation), C.POINTER(_P), C.POINTER(_P), _I, _D, _P, _P, _P],
     "mgb_step_prepare": [_P, C.POINTER(MgbEquation), _D, _P, _P],
+    "mgb_batch_workspace_bytes": [_P, _I, _I, C.POINTER(C.c_size_t)],
+    "mgb_batch_step": [_P, C.POINTER(MgbEquation), C.POINTER(MgbBatch), _I, _D, _P, _P, _P],
     "mgb_step_kernel_count": [_P, C.POINTER(MgbEquation), C.POINTER(_I)],
     "mgb_step_events": [_P, C.POINTER(MgbEquation), C.POINTER(_P), C.POINTER(_P), _I, _D, _P, _P, _P,
                         C.POINTER(_P), _I],

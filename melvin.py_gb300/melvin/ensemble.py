@@ -1,0 +1,152 @@
+"""Ensembles: many independent simulations of one grid advanced together.
+
+Each member is a complete simulation (its own spectral state and
+derivative history); every kernel of a step covers all members at once
+(``mgb_batch_step``), and :meth:`Ensemble.graph` captures several steps
+into one CUDA graph so an ensemble advances ``nsteps`` steps per graph
+launch.  Members live in slots of pooled tensors, so members that start or
+finish at different times can share a batch (see :mod:`melvin.serving`).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .stepper import INTEGRATORS, OPS
+
+
+class FieldSpec:
+    """One advected field: diffusion coefficient, linear terms
+    ``(src, op, coef)`` with src a field index or -1 for psi, and a boundary
+    rule (MGB_BC_* flags)."""
+
+    def __init__(self, kappa, terms=(), bc=0):
+        self.kappa, self.terms, self.bc = float(kappa), list(terms), int(bc)
+
+
+class Ensemble:
+    def __init__(self, params, fields, nslots, integrator=None, order=None, alpha=None, term_coef=None):
+        self.params = params
+        self.plan = N.plan_for(params)
+        self.device = self.plan.device
+        self.F = len(fields)
+        if not 1 <= self.F <= 3:
+            raise ValueError("1 to 3 advected fields")
+        self.nslots = int(nslots)
+        rows, cols = self.plan.spectral_shape
+        order = int(order or params.integrator_order)
+        self.order = order
+        integ = integrator or params.integrator
+        eq = N.MgbEquation()
+        eq.nfields = self.F
+        eq.integrator = INTEGRATORS[integ]
+        eq.order = order
+        eq.alpha = float(params.alpha if alpha is None else alpha)
+        for i, fs in enumerate(fields):
+            fe = eq.f[i]
+            fe.kappa = fs.kappa
+            fe.bc = fs.bc
+            fe.nterms = len(fs.terms)
+            for k, (src, op, coef) in enumerate(fs.terms):
+                fe.terms[k] = N.MgbTerm(int(src), OPS[op] if isinstance(op, str) else int(op), float(coef))
+        self.eq = eq
+        self.q = torch.zeros((self.nslots, self.F, rows, cols), dtype=torch.complex128, device=self.device)
+        self.hist = torch.zeros((self.nslots, self.F, order, rows, cols), dtype=torch.complex128, device=self.device)
+        self.curr = 0
+        self.term_coef = None
+        if term_coef is not None:
+            self.term_coef = torch.as_tensor(term_coef, dtype=torch.float64, device=self.device).reshape(
+                self.nslots, 3, 4).contiguous()
+        b = C.c_size_t()
+        N.check(self.plan.lib.mgb_batch_workspace_bytes(self.plan.handle, self.F, self.nslots, C.byref(b)))
+        self.work = torch.empty(b.value, dtype=torch.uint8, device=self.device)
+        self.diag = torch.zeros((self.nslots, 3), dtype=torch.float64, device=self.device)
+        self._prepared = None
+        self._stepped = False
+
+    # ---- state -----------------------------------------------------------
+    def load_physical(self, slot, arrays):
+        """Load physical fields (one (nx, nz) array per field) into a slot
+        and clear its history."""
+        from .SpectralTransformer import SpectralTransformer
+
+        st = SpectralTransformer(self.params)
+        for f, arr in enumerate(arrays):
+            st.to_spectral(arr, out=self.q[slot, f])
+        self.hist[slot].zero_()
+
+    def reset_history(self, slots=None):
+        if slots is None:
+            self.hist.zero_()
+        else:
+            self.hist[slots] = 0
+
+    # ---- stepping ----------------------------------------------------------
+    def prepare(self, dt):
+        """(Re)compute the update coefficients for `dt` when they are not the
+        ones the plan last prepared for this ensemble's workspace."""
+        if self._prepared != float(dt) or self.plan.last_prepared is not self:
+            self.plan.call("mgb_step_prepare", C.byref(self.eq), float(dt), N.ptr(self.work),
+                           N.stream_handle(self.device))
+            self._prepared = float(dt)
+            self.plan.last_prepared = self
+
+    def _batch(self, members):
+        bt = N.MgbBatch()
+        if members is None:
+            bt.count = self.nslots
+            bt.members = None
+        else:
+            bt.count = int(members.numel())
+            bt.members = members.data_ptr()
+        bt.q = self.q.data_ptr()
+        bt.hist = self.hist.data_ptr()
+        bt.term_coef = None if self.term_coef is None else self.term_coef.data_ptr()
+        return bt
+
+    def step(self, dt, members=None, diagnostics=False):
+        """Advance the listed slots (an int32 device tensor; all slots when
+        None) by one step.  Every member shares ``curr``: members joining a
+        running batch start with a zero history, as a fresh simulation does."""
+        self.prepare(dt)
+        bt = self._batch(members)
+        self.plan.call("mgb_batch_step", C.byref(self.eq), C.byref(bt), self.curr, float(dt), N.ptr(self.work),
+                       N.ptr(self.diag) if diagnostics else None, N.stream_handle(self.device))
+        self.curr = (self.curr + 1) % self.order
+        self._stepped = True
+        return self.diag if diagnostics else None
+
+    def graph(self, dt, nsteps, members=None):
+        """Capture ``nsteps`` steps (a multiple of the integrator order, so
+        the history slot pattern repeats) into a CUDA graph; returns a
+        callable that replays them.  The member list, dt and the equation
+        are fixed at capture."""
+        if nsteps % self.order:
+            raise ValueError(f"nsteps must be a multiple of the integrator order {self.order}")
+        if not self._stepped:
+            raise RuntimeError("advance the ensemble once with step() before capturing: the first launch of "
+                               "each kernel sets attributes that cannot be set inside a capture")
+        self.prepare(dt)
+        curr0 = self.curr
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(device=self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        bt = self._batch(members)
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                for k in range(nsteps):
+                    N.check(self.plan.lib.mgb_batch_step(
+                        self.plan.handle, C.byref(self.eq), C.byref(bt), (curr0 + k) % self.order, float(dt),
+                        N.ptr(self.work), None, C.c_void_p(s.cuda_stream)))
+        torch.cuda.current_stream(self.device).wait_stream(s)
+
+        def replay():
+            g.replay()
+            self.curr = curr0  # nsteps is a multiple of the order
+
+        replay.graph = g
+        return replay

@@ -1,0 +1,64 @@
+"""The continuous-batching server: a request's result is the same alone and
+in a mix (members' arithmetic does not depend on slot, batch composition
+or the shared history slot index; asserted bit-exact), results match the
+oracle, and admission is refused when device memory is short."""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from oracle import problems as P
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfg(precision):
+    from melvin.serving import DDCConfig
+
+    return DDCConfig(Ra_T=1e5, precision=precision)
+
+
+def test_result_same_alone_and_in_mix(cuda):
+    from melvin.serving import Request, Server
+
+    target = Request(rid=0, nx=64, nz=33, r_rho=2.0, nsteps=40, arrival=0.02, seed=7)
+    alone = Server(_cfg("split"), slots_per_block=4).run([target], keep_results=True)[0].result
+    mix = [Request(rid=i + 1, nx=nx, nz=nz, r_rho=1.5 + 0.5 * i, nsteps=30 + 10 * i, arrival=0.0, seed=100 + i)
+           for i, (nx, nz) in enumerate([(64, 33), (32, 17), (64, 33), (128, 65), (64, 33)])]
+    target2 = Request(rid=0, nx=64, nz=33, r_rho=2.0, nsteps=40, arrival=0.02, seed=7)
+    out = Server(_cfg("split"), slots_per_block=4).run(mix + [target2], keep_results=True)
+    res = next(r for r in out if r.rid == 0).result
+    assert np.array_equal(res, alone)
+    assert all(r.finished is not None and r.finished >= r.arrival for r in out)
+
+
+def test_served_result_matches_oracle(cuda):
+    from melvin.serving import Request, Server
+
+    cfg = _cfg("double")
+    req = Request(rid=0, nx=32, nz=17, r_rho=2.5, nsteps=6, seed=3)
+    res = Server(cfg, slots_per_block=2).run([req], keep_results=True)[0].result
+    g = O.Grid(32, 17, cfg.lx, cfg.lz, True, cfg.order)
+    from melvin.workloads import conductive
+
+    t0 = conductive(32, 17, cfg.lx, cfg.lz, seed=6)
+    s0 = conductive(32, 17, cfg.lx, cfg.lz, seed=7)
+    dt = cfg.dt_factor * (cfg.lz / 17) ** 2 / cfg.Pr
+    ref = P.Problem(g, P.ddc_dirichlet_specs(cfg.Pr, cfg.Ra_T, 2.5, cfg.Le),
+                    [np.zeros(g.spectral_shape, complex), O.to_spectral(g, t0), O.to_spectral(g, s0)], dt,
+                    "explicit", 2)
+    for _ in range(6):
+        ref.step()
+    for f in range(3):
+        assert rel_l2(res[f], ref.q[f]) < 1e-12
+
+
+def test_admission_waits_for_memory(cuda, monkeypatch):
+    from melvin.serving import Request, Server
+
+    srv = Server(_cfg("split"), slots_per_block=2)
+    monkeypatch.setattr(torch.cuda, "mem_get_info", lambda device=None: (1 << 20, 1 << 30))
+    assert srv._pool_for(Request(rid=0, nx=64, nz=33, r_rho=2.0, nsteps=1)) is None
+    assert srv.refused == 1 and not srv.pools
