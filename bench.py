@@ -314,22 +314,25 @@ def run_only(args):
     w0 = workloads.decaying_turbulence(n, n, seed=0)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
     sim, w, dw, step = make_run(n, {"fp64": "double"}.get(args.only, args.only), device, w0)
+    tiles = None if args.no_tune else list(step.autotune().tiles)
     for _ in range(args.warmup):
         step.step()
     torch.cuda.synchronize()
     per_step, per_kernel = timed_steps(step, args.steps, flush)
-    print(json.dumps({"only": args.only, "n": n, "steps": args.steps,
+    print(json.dumps({"only": args.only, "n": n, "steps": args.steps, "tiles": tiles,
                       "ms_per_step": round(statistics.mean(per_step), 4),
                       "kernel_ms": [round(statistics.mean(k), 4) for k in per_kernel]}), flush=True)
     return 0
 
 
-def _timed_run(n, precision, device, w0, steps, warmup, flush, dist):
-    """Warm up, then time `steps` fused steps of one precision; returns the
-    per-step and per-kernel times and the stepper."""
+def _timed_run(n, precision, device, w0, steps, warmup, flush, dist, tune=True):
+    """Tune the tile variants (unless `tune` is off), warm up, then time
+    `steps` fused steps of one precision; returns the per-step and
+    per-kernel times, the stepper and the tuning result."""
     import torch
 
     sim, w, dw, step = make_run(n, precision, device, w0)
+    tuned = step.autotune() if tune else None
     for _ in range(warmup):
         step.step()
     torch.cuda.synchronize()
@@ -338,7 +341,22 @@ def _timed_run(n, precision, device, w0, steps, warmup, flush, dist):
     per_step, per_kernel = timed_steps(step, steps, flush)
     torch.cuda.synchronize()
     barrier(dist)
-    return per_step, per_kernel, (sim, w, dw, step)
+    return per_step, per_kernel, (sim, w, dw, step), tuned
+
+
+def _tiles_summary(plan, tuned):
+    """The tile variant used per kernel family, and the tuner's gain."""
+    from melvin._native import FAMILIES
+
+    tiles = plan.get_tiles(1)
+    out = {}
+    for fam, name in enumerate(FAMILIES):
+        _, shape, radix, _ = plan.tile_info(fam, 1, tiles[fam])
+        out[name] = {"variant": tiles[fam], "per_cta": shape, "radix": radix}
+    if tuned is not None:
+        out["tuned"] = {"default_ms": round(tuned.default_ms_per_step, 4), "ms": round(tuned.ms_per_step, 4),
+                        "trials": len(tuned.trials)}
+    return out
 
 
 def _accuracy(n, device, w0, precision, nsteps=100):
@@ -381,11 +399,13 @@ def run_native(args):
     with ClockSampler(local) as clocks:
         t_wall0 = time.perf_counter()
         for key, prec in (("fp64", "double"), ("split", "split"), ("dfloat", "dfloat")):
-            per_step, per_kernel, run = _timed_run(n, prec, device, w0, args.steps, args.warmup, flush, dist)
+            per_step, per_kernel, run, tuned = _timed_run(n, prec, device, w0, args.steps, args.warmup, flush, dist,
+                                                          tune=not args.no_tune)
             secs = reduce_max(sum(per_step) * 1e-3, dist, device)
             model = kernel_model(n, prec == "split")
             roof, kdom = roofline(model, per_kernel, names, peak, peak_kind, traffic, prec)
             results[key] = dict(secs=secs, per_kernel=per_kernel, roof=roof, kdom=kdom, model=model, run=run,
+                                tiles=_tiles_summary(run[3].plan, tuned),
                                 value=aggregate_throughput(n * n, args.steps, world, secs))
             if key == "fp64":
                 wall = time.perf_counter() - t_wall0
@@ -437,7 +457,8 @@ def run_native(args):
             r = results[key]
             return {"value": round(r["value"], 3), "unit": UNIT, "dtype": dtype,
                     "ms_per_step": round(r["secs"] / args.steps * 1e3, 4),
-                    "speedup_vs_fp64": round(r["value"] / r64["value"], 3), "roofline": r["roof"], **acc[key]}
+                    "speedup_vs_fp64": round(r["value"] / r64["value"], 3), "roofline": r["roof"],
+                    "tiles": r["tiles"], **acc[key]}
 
         line = {
             "metric": METRIC, "value": round(r64["value"], 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -446,6 +467,7 @@ def run_native(args):
             "config": dict(WORKLOAD, nx=n, nz=n, l2="flushed (256 MiB write) between timed steps", replicas=world),
             "roofline": r64["roof"],
             "fp64_alu_roof": fp64_roof,
+            "tiles": r64["tiles"],
             "e2e": {"value": round(aggregate_throughput(n * n, args.steps, world, e2e_secs), 3), "unit": UNIT,
                     "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
                     "path": "Stepper.step (FP64) with state and history copied from/to pinned host memory each step"},
@@ -487,6 +509,7 @@ def run_ensemble(args):
         w, c = workloads.kelvin_helmholtz(n, n, deltas[b], seed=b)
         ens.load_physical(b, [w, c])
     ens.step(5e-4)
+    tuned = None if args.no_tune else ens.autotune(5e-4)
     replay = ens.graph(5e-4, graph_steps)
     for _ in range(max(args.warmup, 1)):
         replay()
@@ -516,6 +539,9 @@ def run_ensemble(args):
         "ms_per_ensemble_step": round(ms, 4),
         "hbm": {"algorithmic_bytes_per_step": bytes_step, "achieved_gbs": round(bytes_step / (ms * 1e-3) / 1e9, 1),
                 "peak_gbs": peak, "frac": round(bytes_step / (ms * 1e-3) / 1e9 / peak, 4), "peak_kind": kind},
+        "tiles": list(ens.plan.get_tiles(2)),
+        "tuned": None if tuned is None else {"default_ms": round(tuned.default_ms_per_step, 4),
+                                             "ms": round(tuned.ms_per_step, 4)},
         "l2": "flushed between graph launches"}), flush=True)
     return 0
 
@@ -552,6 +578,7 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
     ap.add_argument("--n", type=int, default=2048, help="grid points per side (default 2048)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default tile variants (no autotuning)")
     ap.add_argument("--only", choices=["fp64", "split", "dfloat"],
                     help="run only the timed fused steps of one precision")
     ap.add_argument("--workload", choices=["turbulence", "kh-ensemble", "serving"], default="turbulence",

@@ -282,6 +282,39 @@ int mgb_step_events(const mgb_plan* plan, const mgb_equation* eq, void* const* q
                     int32_t curr, double dt, void* work, double* diag, void* stream,
                     void* const* events, int32_t nevents);
 
+/* ---- tile variants of the fused step (fully spectral plans) -------------
+ * Each of the three fused-step kernels comes in MGB_TILE_VARIANTS variants
+ * that differ in the work given to one CTA and in the largest FFT radix:
+ *   MGB_FAMILY_XINV, MGB_FAMILY_XFWD (x passes): columns per CTA;
+ *   MGB_FAMILY_ZSTEP (z pass): pairs of grid rows per CTA.
+ * Variant 0 is the default.  An autotuner times the variants on the
+ * caller's workload and sets the fastest per plan and field count.  The
+ * reference leaves the equivalent choice to numpy.fft's internal plan
+ * (melvin/SpectralTransformer.py:58,85,132,191). */
+#define MGB_TILE_VARIANTS 4
+typedef enum mgb_family {
+  MGB_FAMILY_XINV = 0,   /* inverse x pass (velocity and fields to z-mode columns) */
+  MGB_FAMILY_ZSTEP = 1,  /* z pass: to physical rows, products, z stencil, back */
+  MGB_FAMILY_XFWD = 2    /* forward x pass, x stencil, linear terms, update */
+} mgb_family;
+
+typedef struct mgb_tile_info {
+  int32_t available;    /* 1 when the variant exists for this plan (its shared memory fits) */
+  int32_t shape;        /* columns per CTA (x passes) or row pairs per CTA (z pass) */
+  int32_t radix;        /* largest FFT radix (8 or 4) */
+  int32_t reserved;
+  uint64_t smem_bytes;  /* dynamic shared memory per CTA */
+} mgb_tile_info;
+
+/* Describe variant `variant` of `family` for `nfields` advected fields (1..3). */
+int mgb_tile_info_get(const mgb_plan* plan, int32_t family, int32_t nfields, int32_t variant,
+                      mgb_tile_info* info);
+/* Select the variants (tiles[family]) that mgb_step / mgb_batch_step use
+ * for `nfields` advected fields; MGB_ERR_INVALID for an unavailable one. */
+int mgb_plan_set_tiles(mgb_plan* plan, int32_t nfields, const int32_t* tiles);
+/* Read the current selection into tiles[3]. */
+int mgb_plan_get_tiles(const mgb_plan* plan, int32_t nfields, int32_t* tiles);
+
 #ifdef __cplusplus
 }
 #endif

@@ -477,4 +477,47 @@ int mgb_step_events(const mgb_plan* p, const mgb_equation* eq, void* const* q, v
   return step_impl(p, eq, q, hist, curr, dt, work, diag, stream, &et);
 }
 
+static int check_tile_args(const mgb_plan* p, const char* fn, int32_t nfields) {
+  if (p->g.fdm) return fail(MGB_ERR_UNSUPPORTED, "%s: tile variants exist for fully spectral plans only", fn);
+  if (nfields < 1 || nfields > 3) return fail(MGB_ERR_INVALID, "%s: nfields=%d outside 1..3", fn, nfields);
+  return MGB_OK;
+}
+
+int mgb_tile_info_get(const mgb_plan* p, int32_t family, int32_t nfields, int32_t variant, mgb_tile_info* info) {
+  CHECK_PLAN(p);
+  CHECK_PTR(info);
+  if (int st = check_tile_args(p, __func__, nfields)) return st;
+  if (family < 0 || family > 2) return fail(MGB_ERR_INVALID, "%s: family=%d outside 0..2", __func__, family);
+  if (variant < 0 || variant >= MGB_TILE_VARIANTS)
+    return fail(MGB_ERR_INVALID, "%s: variant=%d outside 0..%d", __func__, variant, MGB_TILE_VARIANTS - 1);
+  return fs_tile_info(p, family, nfields, variant, info);
+}
+
+int mgb_plan_set_tiles(mgb_plan* p, int32_t nfields, const int32_t* tiles) {
+  CHECK_PLAN(p);
+  CHECK_PTR(tiles);
+  if (int st = check_tile_args(p, __func__, nfields)) return st;
+  for (int k = 0; k < 3; ++k) {
+    mgb_tile_info info;
+    if (tiles[k] < 0 || tiles[k] >= MGB_TILE_VARIANTS)
+      return fail(MGB_ERR_INVALID, "%s: tiles[%d]=%d outside 0..%d", __func__, k, tiles[k], MGB_TILE_VARIANTS - 1);
+    fs_tile_info(p, k, nfields, tiles[k], &info);
+    if (!info.available)
+      return fail(MGB_ERR_INVALID, "%s: variant %d of family %d does not fit shared memory on this grid", __func__,
+                  tiles[k], k);
+  }
+  std::lock_guard<std::mutex> lock(p->mu);
+  for (int k = 0; k < 3; ++k) p->tiles[nfields - 1][k] = tiles[k];
+  return MGB_OK;
+}
+
+int mgb_plan_get_tiles(const mgb_plan* p, int32_t nfields, int32_t* tiles) {
+  CHECK_PLAN(p);
+  CHECK_PTR(tiles);
+  if (int st = check_tile_args(p, __func__, nfields)) return st;
+  std::lock_guard<std::mutex> lock(p->mu);
+  for (int k = 0; k < 3; ++k) tiles[k] = p->tiles[nfields - 1][k];
+  return MGB_OK;
+}
+
 }  // extern "C"

@@ -74,11 +74,13 @@ struct Dft<8, DIR, T> {
 
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
-// Radix of the pass that starts with sub-transform length NS.
-template <int N, int NS>
+// Radix of the pass that starts with sub-transform length NS, at most RM
+// (8 or 4).  With RM = 8 a remaining length of 16 is split 4 x 4 rather than
+// 8 x 2, so no radix-2 pass follows a radix-8 one.
+template <int N, int NS, int RM>
 struct PassRadix {
   static constexpr int rem = N / NS;
-  static constexpr int value = (rem >= 8 && rem != 16) ? 8 : (rem >= 4 ? 4 : 2);
+  static constexpr int value = (RM >= 8 && rem >= 8 && rem != 16) ? 8 : (rem >= 4 ? 4 : 2);
 };
 
 template <typename T, int N, int C, int CS, int NT, int DIR, int R, int NS>
@@ -120,26 +122,28 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, const cx<T>* __restric
   __syncthreads();
 }
 
-template <typename T, int N, int C, int CS, int NT, int DIR, int NS, bool DONE = (NS >= N)>
+template <typename T, int N, int C, int CS, int NT, int DIR, int RM, int NS, bool DONE = (NS >= N)>
 struct FftPasses {
   static __device__ __forceinline__ void run(cx<T>* buf, const cx<T>* __restrict__ tw) {
-    constexpr int R = PassRadix<N, NS>::value;
+    constexpr int R = PassRadix<N, NS, RM>::value;
     stockham_pass<T, N, C, CS, NT, DIR, R, NS>(buf, tw);
-    FftPasses<T, N, C, CS, NT, DIR, NS * R>::run(buf, tw);
+    FftPasses<T, N, C, CS, NT, DIR, RM, NS * R>::run(buf, tw);
   }
 };
 
-template <typename T, int N, int C, int CS, int NT, int DIR, int NS>
-struct FftPasses<T, N, C, CS, NT, DIR, NS, true> {
+template <typename T, int N, int C, int CS, int NT, int DIR, int RM, int NS>
+struct FftPasses<T, N, C, CS, NT, DIR, RM, NS, true> {
   static __device__ __forceinline__ void run(cx<T>*, const cx<T>* __restrict__) {}
 };
 
-// Transform columns [0, C) of buf (stride CS) in place; the caller must have
-// synchronised after filling buf.  Ends with a __syncthreads().
-template <typename T, int N, int C, int CS, int NT, int DIR>
+// Transform columns [0, C) of buf (stride CS) in place with passes of radix
+// at most RM; the caller must have synchronised after filling buf.  Ends
+// with a __syncthreads().
+template <typename T, int N, int C, int CS, int NT, int DIR, int RM = 8>
 __device__ __forceinline__ void block_fft(cx<T>* buf, const cx<T>* __restrict__ tw) {
   static_assert((N & (N - 1)) == 0 && N >= 4, "power-of-two length");
-  FftPasses<T, N, C, CS, NT, DIR, 1>::run(buf, tw);
+  static_assert(RM == 8 || RM == 4, "maximum radix 8 or 4");
+  FftPasses<T, N, C, CS, NT, DIR, RM, 1>::run(buf, tw);
 }
 
 }  // namespace mgb

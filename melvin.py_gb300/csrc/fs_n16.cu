@@ -1,13 +1,21 @@
-// Transform kernels instantiated for length 16.
-#include "fdm_impl.cuh"
+// Fully spectral kernels for length 16: the FP64 fused-step kernels (every
+// tile variant), the FP64 per-verb kernels, and the launcher table that also
+// takes the FP32 and double-float kernels of fs_n16_f32.cu / fs_n16_df64.cu.
+#include "spectral2d_impl.cuh"
 
 namespace mgb {
+void fill_fs_f32_16(FsLaunchers& L);
+void fill_fs_df64_16(FsLaunchers& L);
+
 const FsLaunchers* fs_launchers_16() {
-  static const FsLaunchers L = make_fs_launchers<16>();
-  return &L;
-}
-const FdLaunchers* fd_launchers_16() {
-  static const FdLaunchers L = make_fd_launchers<16>();
+  static const FsLaunchers L = [] {
+    FsLaunchers l{};
+    fill_step_kernels<double, 16>(l, MGB_PREC_DOUBLE);
+    fill_fs_f32_16(l);
+    fill_fs_df64_16(l);
+    fill_verb_kernels<16>(l);
+    return l;
+  }();
   return &L;
 }
 }  // namespace mgb

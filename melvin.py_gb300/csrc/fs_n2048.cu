@@ -1,13 +1,21 @@
-// Transform kernels instantiated for length 2048.
-#include "fdm_impl.cuh"
+// Fully spectral kernels for length 2048: the FP64 fused-step kernels (every
+// tile variant), the FP64 per-verb kernels, and the launcher table that also
+// takes the FP32 and double-float kernels of fs_n2048_f32.cu / fs_n2048_df64.cu.
+#include "spectral2d_impl.cuh"
 
 namespace mgb {
+void fill_fs_f32_2048(FsLaunchers& L);
+void fill_fs_df64_2048(FsLaunchers& L);
+
 const FsLaunchers* fs_launchers_2048() {
-  static const FsLaunchers L = make_fs_launchers<2048>();
-  return &L;
-}
-const FdLaunchers* fd_launchers_2048() {
-  static const FdLaunchers L = make_fd_launchers<2048>();
+  static const FsLaunchers L = [] {
+    FsLaunchers l{};
+    fill_step_kernels<double, 2048>(l, MGB_PREC_DOUBLE);
+    fill_fs_f32_2048(l);
+    fill_fs_df64_2048(l);
+    fill_verb_kernels<2048>(l);
+    return l;
+  }();
   return &L;
 }
 }  // namespace mgb

@@ -1,0 +1,6 @@
+// Fully spectral fused-step kernels for length 2048 in double-float (default tile).
+#include "spectral2d_impl.cuh"
+
+namespace mgb {
+void fill_fs_df64_2048(FsLaunchers& L) { fill_step_kernels<df64, 2048, 0x1>(L, MGB_PREC_DFLOAT); }
+}  // namespace mgb

@@ -1,13 +1,21 @@
-// Transform kernels instantiated for length 32.
-#include "fdm_impl.cuh"
+// Fully spectral kernels for length 32: the FP64 fused-step kernels (every
+// tile variant), the FP64 per-verb kernels, and the launcher table that also
+// takes the FP32 and double-float kernels of fs_n32_f32.cu / fs_n32_df64.cu.
+#include "spectral2d_impl.cuh"
 
 namespace mgb {
+void fill_fs_f32_32(FsLaunchers& L);
+void fill_fs_df64_32(FsLaunchers& L);
+
 const FsLaunchers* fs_launchers_32() {
-  static const FsLaunchers L = make_fs_launchers<32>();
-  return &L;
-}
-const FdLaunchers* fd_launchers_32() {
-  static const FdLaunchers L = make_fd_launchers<32>();
+  static const FsLaunchers L = [] {
+    FsLaunchers l{};
+    fill_step_kernels<double, 32>(l, MGB_PREC_DOUBLE);
+    fill_fs_f32_32(l);
+    fill_fs_df64_32(l);
+    fill_verb_kernels<32>(l);
+    return l;
+  }();
   return &L;
 }
 }  // namespace mgb

@@ -1,0 +1,6 @@
+// Fully spectral fused-step kernels for length 4096 in FP32 (every tile variant).
+#include "spectral2d_impl.cuh"
+
+namespace mgb {
+void fill_fs_f32_4096(FsLaunchers& L) { fill_step_kernels<float, 4096>(L, MGB_PREC_SPLIT); }
+}  // namespace mgb

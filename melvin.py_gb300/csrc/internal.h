@@ -39,6 +39,8 @@ struct mgb_plan {
   float* tab_f = nullptr;
   void* tab_df = nullptr;  // tux, tuz as double-float
   int device = 0;
+  // Fused-step tile variants [nfields-1][mgb_family] (guarded by mu).
+  int tiles[3][3] = {};
   mutable std::mutex mu;
   mutable PrepRecord prep;
 };
@@ -102,6 +104,8 @@ struct StepBatch {
   const double* tcoef = nullptr;  // optional device [slot][3][4] term coefficients
 };
 
+// Shape of tile variant `v` of a fused-step kernel family (fully spectral).
+int fs_tile_info(const mgb_plan* p, int family, int nfields, int v, mgb_tile_info* out);
 int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb, int curr, double dt, void* work,
                   double* diag, cudaStream_t s, EventTrack* et = nullptr);
 size_t fs_step_workspace(const mgb_plan* p, int nfields);

@@ -64,7 +64,7 @@ int fs_to_physical(const mgb_plan* p, const zd* spec, double* phys, void* work, 
   xa.tw = p->tw_x_d;
   set_tables(p, xa, MGB_PREC_DOUBLE);
   xa.job[0] = XinvJob{spec, SRC_COPY, work, nullptr, nullptr};
-  int st = launched(Lx->xinv[0](xa, 1, 1, s), "to_physical x pass");
+  int st = launched(Lx->xinv[0][0](xa, 1, 1, s), "to_physical x pass");
   if (st) return st;
   ZinvArgs za = {};
   za.g = g;
@@ -112,7 +112,7 @@ int fs_vec_dot_nabla(const mgb_plan* p, const zd* q, double* q_phys, const doubl
   xa.tw = p->tw_x_d;
   set_tables(p, xa, MGB_PREC_DOUBLE);
   xa.job[0] = XinvJob{q, SRC_COPY, w0, nullptr, nullptr};
-  int st = launched(Lx->xinv[0](xa, 1, 1, s), "vec_dot_nabla x pass");
+  int st = launched(Lx->xinv[0][0](xa, 1, 1, s), "vec_dot_nabla x pass");
   if (st) return st;
   ZvdnArgs za = {};
   za.g = g;
@@ -153,7 +153,7 @@ int fs_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* ux_s, zd* uz_s, dou
   set_tables(p, xa, MGB_PREC_DOUBLE);
   xa.job[0] = XinvJob{w, SRC_UX, w0, ux_s, psi};
   xa.job[1] = XinvJob{w, SRC_UZ, w1, uz_s, nullptr};
-  int st = launched(Lx->xinv[0](xa, 2, 1, s), "velocity x pass");
+  int st = launched(Lx->xinv[0][0](xa, 2, 1, s), "velocity x pass");
   if (st) return st;
   ZinvArgs za = {};
   za.g = g;
@@ -281,6 +281,7 @@ int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
   const GridC& g = p->g;
   const int F = eq->nfields;
   const int nb = sb.count;
+  int tile[3];
   {
     // the update coefficients in `work` must be the ones for (eq, dt)
     std::lock_guard<std::mutex> lock(p->mu);
@@ -289,6 +290,7 @@ int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
               pr.order == eq->order && (eq->integrator != MGB_INT_SEMI_IMPLICIT || pr.alpha == eq->alpha);
     for (int f = 0; ok && f < F; ++f) ok = pr.kappa[f] == eq->f[f].kappa;
     if (!ok) return fail(MGB_ERR_INVALID, "mgb_step: call mgb_step_prepare for this equation, dt and workspace first");
+    for (int k = 0; k < 3; ++k) tile[k] = p->tiles[F - 1][k];
   }
   et->mark(s);
   const int prec = p->grid.precision;
@@ -313,7 +315,7 @@ int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
   xa.job[0] = XinvJob{sb.q[0], SRC_UX, w.inter[0], nullptr, nullptr};
   xa.job[1] = XinvJob{sb.q[0], SRC_UZ, w.inter[1], nullptr, nullptr};
   for (int f = 0; f < F; ++f) xa.job[2 + f] = XinvJob{sb.q[f], SRC_COPY, w.inter[2 + f], nullptr, nullptr};
-  int st = launched(Lx->xinv[prec](xa, 2 + F, nb, s), "step x pass");
+  int st = launched(Lx->xinv[prec][tile[MGB_FAMILY_XINV]](xa, 2 + F, nb, s), "step x pass");
   if (st) return st;
   et->mark(s);
 
@@ -329,7 +331,7 @@ int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
   za.partial = diag ? w.partial : nullptr;
   za.fdz = fd_inv(g.sdo, g.dz);
   za.tw = twz;
-  st = launched(Lz->zz_step[prec][F - 1](za, nb, s), "step z pass");
+  st = launched(Lz->zz_step[prec][F - 1][tile[MGB_FAMILY_ZSTEP]](za, nb, s), "step z pass");
   if (st) return st;
   et->mark(s);
 
@@ -361,10 +363,37 @@ int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
   fa.fdx = fd_inv(g.sdo, g.dx);
   fa.inv_norm = 1.0 / ((double)g.nx * (double)g.nz);
   fa.tw = twx;
-  st = launched(Lx->xf_step[prec][F - 1](fa, nb, s), "step forward x pass");
+  st = launched(Lx->xf_step[prec][F - 1][tile[MGB_FAMILY_XFWD]](fa, nb, s), "step forward x pass");
   if (st) return st;
   et->mark(s);
-  if (diag) return pw_finish_diag(w.partial, g.nx / 2, nb, 1.0 / ((double)g.nx * (double)g.nz), diag, s);
+  if (diag) {
+    const int pairs = Lz->zz_shape[prec][F - 1][tile[MGB_FAMILY_ZSTEP]].shape;
+    return pw_finish_diag(w.partial, g.nx / (2 * pairs), nb, 1.0 / ((double)g.nx * (double)g.nz), diag, s);
+  }
+  return MGB_OK;
+}
+
+int fs_tile_info(const mgb_plan* p, int family, int nfields, int v, mgb_tile_info* out) {
+  const GridC& g = p->g;
+  const int prec = p->grid.precision;
+  const FsLaunchers* L = fs_launchers(family == MGB_FAMILY_ZSTEP ? g.nz : g.nx);
+  const TileShape* ts = nullptr;
+  bool have = false;
+  if (family == MGB_FAMILY_XINV) {
+    ts = &L->xinv_shape[prec][v];
+    have = L->xinv[prec][v] != nullptr;
+  } else if (family == MGB_FAMILY_ZSTEP) {
+    ts = &L->zz_shape[prec][nfields - 1][v];
+    have = L->zz_step[prec][nfields - 1][v] != nullptr;
+  } else {
+    ts = &L->xf_shape[prec][nfields - 1][v];
+    have = L->xf_step[prec][nfields - 1][v] != nullptr;
+  }
+  out->available = have ? 1 : 0;
+  out->shape = ts->shape;
+  out->radix = ts->radix;
+  out->reserved = 0;
+  out->smem_bytes = ts->smem;
   return MGB_OK;
 }
 

@@ -48,6 +48,16 @@ struct MinCTAs<df64> {
   static constexpr int value = 2;
 };
 
+// Resident CTAs per SM a kernel asks the register allocator for: MinCTAs,
+// but no more than its shared memory lets reside (228 KB per SM, 1 KB of it
+// reserved per CTA), so a large tile is not squeezed into registers for
+// CTAs that could never be resident together.
+template <typename T, size_t SMEM>
+struct Occ {
+  static constexpr int by_smem = (int)(233472 / (SMEM + 1024));
+  static constexpr int value = by_smem < 1 ? 1 : (by_smem < MinCTAs<T>::value ? by_smem : MinCTAs<T>::value);
+};
+
 // Columns per CTA of an x pass: 4096 complex values in shared memory
 // (64 KB at 16 bytes, 32 KB at 8 bytes, so more FP32 CTAs are resident).
 template <typename T, int N>
@@ -56,6 +66,36 @@ struct XTile {
   static constexpr int C0 = E / N;
   static constexpr int C = C0 < 1 ? 1 : (C0 > 64 ? 64 : C0);
 };
+
+// Tile variants of the fused-step kernels, chosen per plan (and per number
+// of advected fields) by an autotuner that times them on the caller's own
+// workload.  Variant 0 is the default.
+//   x passes (k_xinv, k_xf_step): columns per CTA C and maximum FFT radix
+//     v = 0: C = XTile::C, radix 8; v = 1: C/2; v = 2: 2C; v = 3: C, radix 4
+//   z pass (k_zz_step): row pairs per CTA P and maximum FFT radix
+//     v = 0: P = 1, radix 8; v = 1: P = 2; v = 2: P = 4; v = 3: P = 1, radix 4
+// Variants with the same shape share one kernel; those whose shared memory
+// does not fit are absent.  Columns and row pairs change only which CTA does
+// the work, so they give bit-identical results; the radix changes rounding.
+constexpr int kTileVariants = 4;
+
+template <typename T, int N, int V>
+struct XVar {
+  static constexpr int C0 = XTile<T, N>::C;
+  static constexpr int Cr = V == 1 ? C0 / 2 : (V == 2 ? 2 * C0 : C0);
+  static constexpr int C = Cr < 1 ? 1 : (Cr > 64 ? 64 : Cr);
+  static constexpr int RM = V == 3 ? 4 : 8;
+};
+
+template <int V>
+struct ZVar {
+  static constexpr int P = V == 1 ? 2 : (V == 2 ? 4 : 1);
+  static constexpr int RM = V == 3 ? 4 : 8;
+};
+
+// Largest dynamic shared memory a CTA may request (227 KB minus the static
+// reduction scratch).
+constexpr size_t kMaxDynSmem = 232448 - 1024;
 
 // Batched launches: member z of a launch (the last grid dimension) works on
 // slot = members ? members[z] : z; the arrays of a slot sit at
@@ -110,9 +150,12 @@ struct XinvArgs {
   BatchC b;            // member = blockIdx.z
 };
 
-template <typename T, int N>
-__global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_xinv(const XinvArgs a) {
-  constexpr int C = XTile<T, N>::C;
+// Loads per thread issued together before they are used (latency hiding in
+// the gather loops of the x passes).
+constexpr int kXLoads = 4;
+
+template <typename T, int N, int C, int RM>
+__global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<C>(N) * sizeof(cx<T>)>::value)) k_xinv(const XinvArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const GridC& g = a.g;
@@ -120,31 +163,49 @@ __global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_xinv(const XinvArgs a
   const int m0 = blockIdx.x * C;
   const T* tab = (const T*)(jb.kind == SRC_UX ? a.tux : a.tuz);
   const zd* src = jb.src + (size_t)batch_slot(a.b, blockIdx.z) * a.b.q_stride;
-  for (int e = threadIdx.x; e < sbuf_elems<C>(N); e += NT) buf[e] = mk<T>(0, 0);
-  __syncthreads();
-  for (int e = threadIdx.x; e < g.rows * C; e += NT) {
-    const int r = e / C, c = e - r * C, m = m0 + c;
-    if (m >= g.cols) continue;
-    const size_t idx = (size_t)r * g.cols + m;
-    const zd w = src[idx];
-    const cx<T> wt = cvt<T>(w);
-    cx<T> v = wt;
-    if (jb.kind == SRC_UX) {
-      const T t = tab[idx];
-      v = mk(-(t * wt.y), t * wt.x);
-    } else if (jb.kind == SRC_UZ) {
-      const T t = tab[idx];
-      v = mk(t * wt.y, -(t * wt.x));
+  // zero the 2/3-rule gap rows nn+1 .. N-nn-1 (the kept rows are written below)
+  for (int e = threadIdx.x; e < (N - g.rows) * C; e += NT) {
+    const int x = g.nn + 1 + e / C, c = e % C;
+    buf[sx<C>(x, c)] = mk<T>(0, 0);
+  }
+  const int total = g.rows * C;
+  for (int e0 = threadIdx.x; e0 < total; e0 += NT * kXLoads) {
+    zd w[kXLoads];
+    T t[kXLoads];
+#pragma unroll
+    for (int u = 0; u < kXLoads; ++u) {
+      const int e = e0 + u * NT;
+      const int r = e / C, m = m0 + (e - r * C);
+      const bool ok = e < total && m < g.cols;
+      const size_t idx = (size_t)r * g.cols + m;
+      w[u] = ok ? src[idx] : mk(0.0, 0.0);
+      t[u] = (ok && jb.kind != SRC_COPY) ? tab[idx] : (T)0;
     }
-    if (jb.spec_out) jb.spec_out[idx] = cvt<double>(v);
-    if (jb.psi_out) {
-      const double rl = a.rlap[idx];
-      jb.psi_out[idx] = mk(-(w.x * rl), -(w.y * rl));
+#pragma unroll
+    for (int u = 0; u < kXLoads; ++u) {
+      const int e = e0 + u * NT;
+      if (e >= total) break;
+      const int r = e / C, c = e - r * C, m = m0 + c;
+      const size_t idx = (size_t)r * g.cols + m;
+      const cx<T> wt = cvt<T>(w[u]);
+      cx<T> v = wt;
+      if (jb.kind == SRC_UX) {
+        v = mk(-(t[u] * wt.y), t[u] * wt.x);
+      } else if (jb.kind == SRC_UZ) {
+        v = mk(t[u] * wt.y, -(t[u] * wt.x));
+      }
+      if (m < g.cols) {
+        if (jb.spec_out) jb.spec_out[idx] = cvt<double>(v);
+        if (jb.psi_out) {
+          const double rl = a.rlap[idx];
+          jb.psi_out[idx] = mk(-(w[u].x * rl), -(w[u].y * rl));
+        }
+      }
+      buf[sx<C>(row_bin(r, g.nn, N), c)] = v;  // zero for columns past the last mode
     }
-    buf[sx<C>(row_bin(r, g.nn, N), c)] = v;
   }
   __syncthreads();
-  block_fft<T, N, C, C, NT, +1>(buf, (const cx<T>*)a.tw);
+  block_fft<T, N, C, C, NT, +1, RM>(buf, (const cx<T>*)a.tw);
   cx<T>* out = (cx<T>*)((char*)jb.out + (size_t)blockIdx.z * a.b.inter_stride);
   for (int e = threadIdx.x; e < N * C; e += NT) {
     const int x = e / C, c = e - x * C, m = m0 + c;
@@ -243,12 +304,15 @@ __device__ __forceinline__ void block_diag(double s, double mx, double mz, doubl
 }
 
 // ---------------------------------------------------------------------------
-// Fused z pass of the timestep: for rows x0 = 2*blockIdx.x and x0+1,
+// Fused z pass of the timestep: for P row pairs (rows x0 = 2*(P*blockIdx.x+p)
+// and x0+1, p < P),
 //   inverse c2r of ux, uz and the F advected fields,
 //   a_f = ux * q_f, b_f = uz * q_f, c_f = d/dz b_f (periodic stencil),
 //   forward r2c of a_f + i c_f, keep the nm leading modes.
-// Outputs may alias the inputs: a CTA reads only its own two rows, before it
-// writes them.
+// Pair p's inputs sit in columns p*NIN + i and its outputs in p*NOUT + j of
+// the CTA's buffer; a thread reads every input of a position z before it
+// writes that position's outputs.  Outputs may alias the inputs: a CTA reads
+// only its own rows, before it writes them.
 // ---------------------------------------------------------------------------
 
 struct ZzArgs {
@@ -265,74 +329,95 @@ struct ZzArgs {
   BatchC b;           // member = blockIdx.y
 };
 
-template <typename T, int N, int F>
-__global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_zz_step(const ZzArgs a) {
-  constexpr int NIN = 2 + F, NOUT = 2 * F;
-  constexpr int CS = NIN > NOUT ? NIN : NOUT;
+template <int F, int P>
+struct ZzShape {
+  static constexpr int NIN = 2 + F, NOUT = 2 * F;
+  static constexpr int CS = P * (NIN > NOUT ? NIN : NOUT);
+};
+
+template <typename T, int N, int F, int P, int RM>
+__global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<ZzShape<F, P>::CS>(N) * sizeof(cx<T>)>::value))
+    k_zz_step(const ZzArgs a) {
+  constexpr int NIN = ZzShape<F, P>::NIN, NOUT = ZzShape<F, P>::NOUT, CS = ZzShape<F, P>::CS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const GridC& g = a.g;
-  const int x0 = 2 * blockIdx.x;
+  const int xb = 2 * P * blockIdx.x;
   const int nm = g.cols, ld = a.ld;
   const size_t moff = (size_t)blockIdx.y * a.b.inter_stride;
-  const size_t r0 = (size_t)x0 * ld, r1 = r0 + ld;
-  for (int e = threadIdx.x; e < sbuf_elems<CS>(N); e += NT) buf[e] = mk<T>(0, 0);
-  __syncthreads();
+  // zero the modes nm .. N-nm of the input columns (the rest is written below)
+  for (int e = threadIdx.x; e < (N - 2 * nm + 1) * P * NIN; e += NT) {
+    const int z = nm + e / (P * NIN), c = e % (P * NIN);
+    buf[sx<CS>(z, c)] = mk<T>(0, 0);
+  }
   {
     const cx<T>* ux = (const cx<T>*)((const char*)a.in[0] + moff);
     const cx<T>* uz = (const cx<T>*)((const char*)a.in[1] + moff);
     for (int m = threadIdx.x; m < nm; m += NT) {
-      put_pair<T, N, CS>(buf, 0, m, ux[r0 + m], uz[r0 + m]);
-      put_pair<T, N, CS>(buf, 1, m, ux[r1 + m], uz[r1 + m]);
 #pragma unroll
-      for (int f = 0; f < F; ++f) {
-        const cx<T>* q = (const cx<T>*)((const char*)a.in[2 + f] + moff);
-        put_pair<T, N, CS>(buf, 2 + f, m, q[r0 + m], q[r1 + m]);
+      for (int p = 0; p < P; ++p) {
+        const size_t r0 = (size_t)(xb + 2 * p) * ld, r1 = r0 + ld;
+        put_pair<T, N, CS>(buf, p * NIN + 0, m, ux[r0 + m], uz[r0 + m]);
+        put_pair<T, N, CS>(buf, p * NIN + 1, m, ux[r1 + m], uz[r1 + m]);
+#pragma unroll
+        for (int f = 0; f < F; ++f) {
+          const cx<T>* q = (const cx<T>*)((const char*)a.in[2 + f] + moff);
+          put_pair<T, N, CS>(buf, p * NIN + 2 + f, m, q[r0 + m], q[r1 + m]);
+        }
       }
     }
   }
   __syncthreads();
-  block_fft<T, N, NIN, CS, NT, +1>(buf, (const cx<T>*)a.tw);
+  block_fft<T, N, P * NIN, CS, NT, +1, RM>(buf, (const cx<T>*)a.tw);
 
   double ke = 0.0, mx = -INFINITY, mz = -INFINITY;
   for (int z = threadIdx.x; z < N; z += NT) {
-    cx<T> w[NIN];
+    cx<T> w[P * NIN];
 #pragma unroll
-    for (int c = 0; c < NIN; ++c) w[c] = buf[sx<CS>(z, c)];
-    const T ux0 = w[0].x, uz0 = w[0].y, ux1 = w[1].x, uz1 = w[1].y;
-    if (a.ux_phys) {
-      a.ux_phys[(size_t)x0 * N + z] = (double)ux0;
-      a.ux_phys[(size_t)(x0 + 1) * N + z] = (double)ux1;
-      a.uz_phys[(size_t)x0 * N + z] = (double)uz0;
-      a.uz_phys[(size_t)(x0 + 1) * N + z] = (double)uz1;
-    }
-    if (a.partial) {
-      const double dx0 = (double)ux0, dz0 = (double)uz0, dx1 = (double)ux1, dz1 = (double)uz1;
-      ke += (dz0 * dz0 + dx0 * dx0) + (dz1 * dz1 + dx1 * dx1);
-      mx = nan_max(nan_max(mx, dx0), dx1);
-      mz = nan_max(nan_max(mz, dz0), dz1);
-    }
+    for (int c = 0; c < P * NIN; ++c) w[c] = buf[sx<CS>(z, c)];
 #pragma unroll
-    for (int f = 0; f < F; ++f) {
-      const T q0 = w[2 + f].x, q1 = w[2 + f].y;
-      buf[sx<CS>(z, f)] = mk(ux0 * q0, uz0 * q0);
-      buf[sx<CS>(z, F + f)] = mk(ux1 * q1, uz1 * q1);
+    for (int p = 0; p < P; ++p) {
+      const cx<T>* wp = w + p * NIN;
+      const int x0 = xb + 2 * p;
+      const T ux0 = wp[0].x, uz0 = wp[0].y, ux1 = wp[1].x, uz1 = wp[1].y;
+      if (a.ux_phys) {
+        a.ux_phys[(size_t)x0 * N + z] = (double)ux0;
+        a.ux_phys[(size_t)(x0 + 1) * N + z] = (double)ux1;
+        a.uz_phys[(size_t)x0 * N + z] = (double)uz0;
+        a.uz_phys[(size_t)(x0 + 1) * N + z] = (double)uz1;
+      }
+      if (a.partial) {
+        const double dx0 = (double)ux0, dz0 = (double)uz0, dx1 = (double)ux1, dz1 = (double)uz1;
+        ke += (dz0 * dz0 + dx0 * dx0) + (dz1 * dz1 + dx1 * dx1);
+        mx = nan_max(nan_max(mx, dx0), dx1);
+        mz = nan_max(nan_max(mz, dz0), dz1);
+      }
+#pragma unroll
+      for (int f = 0; f < F; ++f) {
+        const T q0 = wp[2 + f].x, q1 = wp[2 + f].y;
+        buf[sx<CS>(z, p * NOUT + f)] = mk(ux0 * q0, uz0 * q0);
+        buf[sx<CS>(z, p * NOUT + F + f)] = mk(ux1 * q1, uz1 * q1);
+      }
     }
   }
   __syncthreads();
-  fd_imag_columns<T, N, CS, NOUT>(buf, g.sdo, (T)a.fdz);
-  block_fft<T, N, NOUT, CS, NT, -1>(buf, (const cx<T>*)a.tw);
+  fd_imag_columns<T, N, CS, P * NOUT>(buf, g.sdo, (T)a.fdz);
+  block_fft<T, N, P * NOUT, CS, NT, -1, RM>(buf, (const cx<T>*)a.tw);
   for (int m = threadIdx.x; m < nm; m += NT) {
 #pragma unroll
-    for (int f = 0; f < F; ++f) {
-      cx<T>* ao = (cx<T>*)((char*)a.aout[f] + moff);
-      cx<T>* co = (cx<T>*)((char*)a.cout[f] + moff);
+    for (int p = 0; p < P; ++p) {
+      const size_t r0 = (size_t)(xb + 2 * p) * ld, r1 = r0 + ld;
 #pragma unroll
-      for (int rho = 0; rho < 2; ++rho) {
-        cx<T> A, Cc;
-        get_pair<T, N, CS>(buf, rho * F + f, m, A, Cc);
-        ao[(rho ? r1 : r0) + m] = A;
-        co[(rho ? r1 : r0) + m] = Cc;
+      for (int f = 0; f < F; ++f) {
+        cx<T>* ao = (cx<T>*)((char*)a.aout[f] + moff);
+        cx<T>* co = (cx<T>*)((char*)a.cout[f] + moff);
+#pragma unroll
+        for (int rho = 0; rho < 2; ++rho) {
+          cx<T> A, Cc;
+          get_pair<T, N, CS>(buf, p * NOUT + rho * F + f, m, A, Cc);
+          ao[(rho ? r1 : r0) + m] = A;
+          co[(rho ? r1 : r0) + m] = Cc;
+        }
       }
     }
   }
@@ -401,42 +486,72 @@ __device__ __forceinline__ zd lin_term(const GridC& g, zd s, int op, int n, int 
 }
 
 // Weighted Adams-Bashforth sum 3 f0 - f1 (AB2) or
-// 55 f0 - 59 f1 + 37 f2 - 9 f3 (AB4) (melvin/Integrator.py:5-18); the dt/2
-// or dt/24 factor is part of the update coefficients.
-__device__ __forceinline__ zd ab_sum(const zd* h, size_t slot, int order, int curr, zd f0) {
-  if (order == 2) {
-    const zd f1 = h[(size_t)((curr + 1) & 1) * slot];
-    return mk(3 * f0.x - f1.x, 3 * f0.y - f1.y);
-  }
-  const zd f1 = h[(size_t)((curr + 3) & 3) * slot];
-  const zd f2 = h[(size_t)((curr + 2) & 3) * slot];
-  const zd f3 = h[(size_t)((curr + 1) & 3) * slot];
-  return mk(((55 * f0.x - 59 * f1.x) + 37 * f2.x) - 9 * f3.x, ((55 * f0.y - 59 * f1.y) + 37 * f2.y) - 9 * f3.y);
+// 55 f0 - 59 f1 + 37 f2 - 9 f3 (AB4) (melvin/Integrator.py:5-18) of the
+// newest value f0 and the previous ones hp[i] = f_{-1-i}; the dt/2 or dt/24
+// factor is part of the update coefficients.
+__device__ __forceinline__ zd ab_sum(int order, zd f0, const zd* hp) {
+  if (order == 2) return mk(3 * f0.x - hp[0].x, 3 * f0.y - hp[0].y);
+  return mk(((55 * f0.x - 59 * hp[0].x) + 37 * hp[1].x) - 9 * hp[2].x,
+            ((55 * f0.y - 59 * hp[0].y) + 37 * hp[1].y) - 9 * hp[2].y);
 }
 
-template <typename T, int N, int F>
-__global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_xf_step(const XfArgs a) {
-  constexpr int C = XTile<T, N>::C;
+// Elements per thread whose state, coefficient and history loads the update
+// loop of k_xf_step issues together (F fields x up to 5 complex doubles each).
+template <int F>
+struct XfLoads {
+  static constexpr int value = F == 1 ? 2 : 1;
+};
+
+template <typename T, int N, int F, int C, int RM>
+__global__ void __launch_bounds__(NT, (Occ<T, F * sbuf_elems<C>(N) * sizeof(cx<T>)>::value))
+    k_xf_step(const XfArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const GridC& g = a.g;
   const int m0 = blockIdx.x * C;
   const int sdo = g.sdo;
+  const T fdx = (T)a.fdx;
   const size_t moff = (size_t)blockIdx.y * a.b.inter_stride;
   const int mslot = batch_slot(a.b, blockIdx.y);
+  // J_f = d/dx(A_f) + C_f: periodic x stencil along each column
 #pragma unroll
   for (int f = 0; f < F; ++f) {
     const cx<T>* A = (const cx<T>*)((const char*)a.ain[f] + moff);
     const cx<T>* Cc = (const cx<T>*)((const char*)a.cin[f] + moff);
     cx<T>* bf = buf + f * sbuf_elems<C>(N);
-    for (int e = threadIdx.x; e < N * C; e += NT) {
-      const int x = e / C, c = e - x * C, m = m0 + c;
-      bf[sx<C>(x, c)] = (m < g.cols) ? jac_x<T, N>(A, Cc, x, m, a.ld, sdo, (T)a.fdx) : mk<T>(0, 0);
+    for (int e0 = threadIdx.x; e0 < N * C; e0 += NT * kXLoads) {
+      cx<T> p1[kXLoads], m1[kXLoads], p2[kXLoads], m2[kXLoads], cc[kXLoads];
+#pragma unroll
+      for (int u = 0; u < kXLoads; ++u) {
+        const int e = e0 + u * NT;
+        const int x = e / C, m = m0 + (e - x * C);
+        const bool ok = e < N * C && m < g.cols;
+        const bool o4 = ok && sdo != 2;
+        const cx<T> z0 = mk<T>(0, 0);
+        p1[u] = ok ? A[(size_t)((x + 1) & (N - 1)) * a.ld + m] : z0;
+        m1[u] = ok ? A[(size_t)((x - 1) & (N - 1)) * a.ld + m] : z0;
+        p2[u] = o4 ? A[(size_t)((x + 2) & (N - 1)) * a.ld + m] : z0;
+        m2[u] = o4 ? A[(size_t)((x - 2) & (N - 1)) * a.ld + m] : z0;
+        cc[u] = ok ? Cc[(size_t)x * a.ld + m] : z0;
+      }
+#pragma unroll
+      for (int u = 0; u < kXLoads; ++u) {
+        const int e = e0 + u * NT;
+        if (e >= N * C) break;
+        const int x = e / C, c = e - x * C;
+        cx<T> d;
+        if (sdo == 2) {
+          d = (p1[u] - m1[u]) * fdx;
+        } else {
+          d = (((p2[u] * (T)-0.25 + p1[u] * (T)2) - m1[u] * (T)2) + m2[u] * (T)0.25) * fdx;
+        }
+        bf[sx<C>(x, c)] = d + cc[u];  // zero for columns past the last mode
+      }
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int f = 0; f < F; ++f) block_fft<T, N, C, C, NT, -1>(buf + f * sbuf_elems<C>(N), (const cx<T>*)a.tw);
+  for (int f = 0; f < F; ++f) block_fft<T, N, C, C, NT, -1, RM>(buf + f * sbuf_elems<C>(N), (const cx<T>*)a.tw);
 
   // -1/(nx*nz) is a power of two for the grids built, so scaling in T is exact
   const T neg_norm = (T)(-a.inv_norm);
@@ -449,51 +564,74 @@ __global__ void __launch_bounds__(NT, MinCTAs<T>::value) k_xf_step(const XfArgs 
     hf[f] = a.hist[f] + (size_t)mslot * a.b.h_stride;
   }
   const double* tco = a.b.tcoef ? a.b.tcoef + (size_t)mslot * 12 : nullptr;
-  for (int e = threadIdx.x; e < g.rows * C; e += NT) {
-    const int r = e / C, c = e - r * C, m = m0 + c;
-    if (m >= g.cols) continue;
-    const int n = row_mode(r, g.nn), k = row_bin(r, g.nn, N);
-    const size_t idx = (size_t)r * g.cols + m;
-    zd qo[F];
+  const bool ab4 = a.order != 2;
+  // history slots of f_{-1}, f_{-2}, f_{-3} (melvin/TimeDerivative.py:4-65)
+  const size_t hs0 = (size_t)(ab4 ? ((a.curr + 3) & 3) : ((a.curr + 1) & 1)) * slot;
+  const size_t hs1 = (size_t)((a.curr + 2) & 3) * slot, hs2 = (size_t)((a.curr + 1) & 3) * slot;
+  constexpr int U = XfLoads<F>::value;
+  const int total = g.rows * C;
+  for (int e0 = threadIdx.x; e0 < total; e0 += NT * U) {
+    zd qo[U][F], cf[U][F], hp[U][F][3];
+    double rl[U];
 #pragma unroll
-    for (int f = 0; f < F; ++f) qo[f] = qf[f][idx];
-    zd psi = mk(0.0, 0.0);
-    if (a.need_psi) {
-      const double rl = a.rlap[idx];
-      psi = mk(-(qo[0].x * rl), -(qo[0].y * rl));
+    for (int u = 0; u < U; ++u) {
+      const int e = e0 + u * NT;
+      const int r = e / C, m = m0 + (e - r * C);
+      const bool ok = e < total && m < g.cols;
+      const size_t idx = (size_t)r * g.cols + m;
+      const zd z0 = mk(0.0, 0.0);
+      rl[u] = (ok && a.need_psi) ? a.rlap[idx] : 0.0;
+#pragma unroll
+      for (int f = 0; f < F; ++f) {
+        qo[u][f] = ok ? qf[f][idx] : z0;
+        cf[u][f] = ok ? a.coef[f][idx] : z0;
+        hp[u][f][0] = ok ? hf[f][hs0 + idx] : z0;
+        hp[u][f][1] = (ok && ab4) ? hf[f][hs1 + idx] : z0;
+        hp[u][f][2] = (ok && ab4) ? hf[f][hs2 + idx] : z0;
+      }
     }
 #pragma unroll
-    for (int f = 0; f < F; ++f) {
-      const XfField& eq = a.eq[f];
-      // dq[:] = -q.vec_dot_nabla(...) + linear terms
-      const cx<T> J = buf[f * sbuf_elems<C>(N) + sx<C>(k, c)] * neg_norm;
-      zd fv = cvt<double>(J);
-      for (int t = 0; t < eq.nterms; ++t) {
-        const int sidx = eq.tsrc[t];
-        zd s = psi;
+    for (int u = 0; u < U; ++u) {
+      const int e = e0 + u * NT;
+      const int r = e / C, c = e - r * C, m = m0 + c;
+      if (e >= total || m >= g.cols) continue;
+      const int n = row_mode(r, g.nn), k = row_bin(r, g.nn, N);
+      const size_t idx = (size_t)r * g.cols + m;
+      zd psi = mk(0.0, 0.0);
+      if (a.need_psi) psi = mk(-(qo[u][0].x * rl[u]), -(qo[u][0].y * rl[u]));
 #pragma unroll
-        for (int q2 = 0; q2 < F; ++q2)
-          if (sidx == q2) s = qo[q2];
-        const zd v = lin_term(g, s, eq.top[t], n, m);
-        const double cc = tco ? tco[f * 4 + t] : eq.tcoef[t];
-        fv = mk(fv.x + cc * v.x, fv.y + cc * v.y);
+      for (int f = 0; f < F; ++f) {
+        const XfField& eq = a.eq[f];
+        // dq[:] = -q.vec_dot_nabla(...) + linear terms
+        const cx<T> J = buf[f * sbuf_elems<C>(N) + sx<C>(k, c)] * neg_norm;
+        zd fv = cvt<double>(J);
+        for (int t = 0; t < eq.nterms; ++t) {
+          const int sidx = eq.tsrc[t];
+          zd sv = psi;
+#pragma unroll
+          for (int q2 = 0; q2 < F; ++q2)
+            if (sidx == q2) sv = qo[u][q2];
+          const zd v = lin_term(g, sv, eq.top[t], n, m);
+          const double cc = tco ? tco[f * 4 + t] : eq.tcoef[t];
+          fv = mk(fv.x + cc * v.x, fv.y + cc * v.y);
+        }
+        const zd cff = cf[u][f], q0 = qo[u][f];
+        zd qn;
+        if (a.integrator == MGB_INT_SEMI_IMPLICIT) {
+          // q' = ((1 + (1-a) dt L) q + AB) / (1 - a dt L) = cf.x q + cf.y * sum
+          hf[f][(size_t)a.curr * slot + idx] = fv;
+          const zd sm = ab_sum(a.order, fv, hp[u][f]);
+          qn = mk(cff.x * q0.x + cff.y * sm.x, cff.x * q0.y + cff.y * sm.y);
+        } else {
+          // explicit: the history keeps N + D, D = kappa * snabla2(q) = cf.x q
+          fv = mk(fv.x + cff.x * q0.x, fv.y + cff.x * q0.y);
+          hf[f][(size_t)a.curr * slot + idx] = fv;
+          const zd sm = ab_sum(a.order, fv, hp[u][f]);
+          qn = mk(q0.x + cff.y * sm.x, q0.y + cff.y * sm.y);
+        }
+        if ((eq.bc & MGB_BC_ZERO_M0) && m == 0) qn = mk(0.0, 0.0);
+        qf[f][idx] = qn;
       }
-      const zd cf = a.coef[f][idx];
-      zd qn;
-      if (a.integrator == MGB_INT_SEMI_IMPLICIT) {
-        // q' = ((1 + (1-a) dt L) q + AB) / (1 - a dt L) = cf.x q + cf.y * sum
-        hf[f][(size_t)a.curr * slot + idx] = fv;
-        const zd sm = ab_sum(hf[f] + idx, slot, a.order, a.curr, fv);
-        qn = mk(cf.x * qo[f].x + cf.y * sm.x, cf.x * qo[f].y + cf.y * sm.y);
-      } else {
-        // explicit: the history keeps N + D, D = kappa * snabla2(q) = cf.x q
-        fv = mk(fv.x + cf.x * qo[f].x, fv.y + cf.x * qo[f].y);
-        hf[f][(size_t)a.curr * slot + idx] = fv;
-        const zd sm = ab_sum(hf[f] + idx, slot, a.order, a.curr, fv);
-        qn = mk(qo[f].x + cf.y * sm.x, qo[f].y + cf.y * sm.y);
-      }
-      if ((eq.bc & MGB_BC_ZERO_M0) && m == 0) qn = mk(0.0, 0.0);
-      qf[f][idx] = qn;
     }
   }
 }
@@ -677,47 +815,35 @@ inline cudaError_t prep_smem(K kernel, size_t smem) {
   return e;
 }
 
-template <typename T, int N>
+template <typename T, int N, int V>
 cudaError_t launch_xinv(const XinvArgs& a, int njobs, int nb, cudaStream_t s) {
-  constexpr int C = XTile<T, N>::C;
+  constexpr int C = XVar<T, N, V>::C, RM = XVar<T, N, V>::RM;
   const size_t smem = (size_t)sbuf_elems<C>(N) * sizeof(cx<T>);
-  cudaError_t e = prep_smem(k_xinv<T, N>, smem);
+  cudaError_t e = prep_smem(k_xinv<T, N, C, RM>, smem);
   if (e != cudaSuccess) return e;
   dim3 grid((a.g.cols + C - 1) / C, njobs, nb);
-  k_xinv<T, N><<<grid, NT, smem, s>>>(a);
+  k_xinv<T, N, C, RM><<<grid, NT, smem, s>>>(a);
   return cudaGetLastError();
 }
 
-// Largest dynamic shared memory a CTA may request (227 KB minus the static
-// reduction scratch).
-constexpr size_t kMaxDynSmem = 232448 - 1024;
-
-template <typename T, int N, int F>
+template <typename T, int N, int F, int V>
 cudaError_t launch_zz_step(const ZzArgs& a, int nb, cudaStream_t s) {
-  constexpr int CS = (2 + F) > (2 * F) ? (2 + F) : (2 * F);
-  constexpr size_t smem = (size_t)sbuf_elems<CS>(N) * sizeof(cx<T>);
-  if constexpr (smem > kMaxDynSmem) {
-    return cudaErrorInvalidConfiguration;
-  } else {
-    cudaError_t e = prep_smem(k_zz_step<T, N, F>, smem);
-    if (e != cudaSuccess) return e;
-    k_zz_step<T, N, F><<<dim3(a.g.nx / 2, nb), NT, smem, s>>>(a);
-    return cudaGetLastError();
-  }
+  constexpr int P = ZVar<V>::P, RM = ZVar<V>::RM;
+  const size_t smem = (size_t)sbuf_elems<ZzShape<F, P>::CS>(N) * sizeof(cx<T>);
+  cudaError_t e = prep_smem(k_zz_step<T, N, F, P, RM>, smem);
+  if (e != cudaSuccess) return e;
+  k_zz_step<T, N, F, P, RM><<<dim3(a.g.nx / (2 * P), nb), NT, smem, s>>>(a);
+  return cudaGetLastError();
 }
 
-template <typename T, int N, int F>
+template <typename T, int N, int F, int V>
 cudaError_t launch_xf_step(const XfArgs& a, int nb, cudaStream_t s) {
-  constexpr int C = XTile<T, N>::C;
-  constexpr size_t smem = (size_t)F * sbuf_elems<C>(N) * sizeof(cx<T>);
-  if constexpr (smem > kMaxDynSmem) {
-    return cudaErrorInvalidConfiguration;
-  } else {
-    cudaError_t e = prep_smem(k_xf_step<T, N, F>, smem);
-    if (e != cudaSuccess) return e;
-    k_xf_step<T, N, F><<<dim3((a.g.cols + C - 1) / C, nb), NT, smem, s>>>(a);
-    return cudaGetLastError();
-  }
+  constexpr int C = XVar<T, N, V>::C, RM = XVar<T, N, V>::RM;
+  const size_t smem = (size_t)F * sbuf_elems<C>(N) * sizeof(cx<T>);
+  cudaError_t e = prep_smem(k_xf_step<T, N, F, C, RM>, smem);
+  if (e != cudaSuccess) return e;
+  k_xf_step<T, N, F, C, RM><<<dim3((a.g.cols + C - 1) / C, nb), NT, smem, s>>>(a);
+  return cudaGetLastError();
 }
 
 template <int N, int NF>
@@ -757,47 +883,117 @@ cudaError_t launch_xf_out(const XfOutArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// Shape of one tile variant of a fused-step kernel: columns (x passes) or
+// row pairs (z pass) per CTA, maximum FFT radix and dynamic shared memory;
+// smem == 0 marks a variant whose shared memory does not fit.
+struct TileShape {
+  int shape, radix;
+  size_t smem;
+};
+
 // Table of launchers for one length N, filled by the per-N translation units.
 struct FsLaunchers {
-  cudaError_t (*xinv[3])(const XinvArgs&, int, int, cudaStream_t);  // [precision](args, jobs, members)
-  cudaError_t (*zz_step[3][3])(const ZzArgs&, int, cudaStream_t);    // [precision][F-1](args, members)
-  cudaError_t (*xf_step[3][3])(const XfArgs&, int, cudaStream_t);
+  // [precision][variant](args, jobs, members)
+  cudaError_t (*xinv[3][kTileVariants])(const XinvArgs&, int, int, cudaStream_t);
+  // [precision][F-1][variant](args, members)
+  cudaError_t (*zz_step[3][3][kTileVariants])(const ZzArgs&, int, cudaStream_t);
+  cudaError_t (*xf_step[3][3][kTileVariants])(const XfArgs&, int, cudaStream_t);
+  TileShape xinv_shape[3][kTileVariants];
+  TileShape zz_shape[3][3][kTileVariants];
+  TileShape xf_shape[3][3][kTileVariants];
   cudaError_t (*zinv_phys[2])(const ZinvArgs&, cudaStream_t);        // [NF-1]
   cudaError_t (*zfwd_phys)(const ZfwdArgs&, cudaStream_t);
   cudaError_t (*zz_vdn)(const ZvdnArgs&, cudaStream_t);
   cudaError_t (*xf_out)(const XfOutArgs&, cudaStream_t);
 };
 
+template <typename T, int N, int V>
+void fill_xinv(FsLaunchers& L, int prec) {
+  constexpr int C = XVar<T, N, V>::C;
+  constexpr size_t smem = (size_t)sbuf_elems<C>(N) * sizeof(cx<T>);
+  L.xinv_shape[prec][V] = TileShape{C, XVar<T, N, V>::RM, smem <= kMaxDynSmem ? smem : 0};
+  if constexpr (smem <= kMaxDynSmem) {
+    L.xinv[prec][V] = launch_xinv<T, N, V>;
+  } else {
+    L.xinv[prec][V] = nullptr;
+  }
+}
+
+template <typename T, int N, int F, int V>
+void fill_zz(FsLaunchers& L, int prec) {
+  constexpr int P = ZVar<V>::P;
+  constexpr size_t smem = (size_t)sbuf_elems<ZzShape<F, P>::CS>(N) * sizeof(cx<T>);
+  L.zz_shape[prec][F - 1][V] = TileShape{P, ZVar<V>::RM, smem <= kMaxDynSmem ? smem : 0};
+  if constexpr (smem <= kMaxDynSmem) {
+    L.zz_step[prec][F - 1][V] = launch_zz_step<T, N, F, V>;
+  } else {
+    L.zz_step[prec][F - 1][V] = nullptr;
+  }
+}
+
+template <typename T, int N, int F, int V>
+void fill_xf(FsLaunchers& L, int prec) {
+  constexpr int C = XVar<T, N, V>::C;
+  constexpr size_t smem = (size_t)F * sbuf_elems<C>(N) * sizeof(cx<T>);
+  L.xf_shape[prec][F - 1][V] = TileShape{C, XVar<T, N, V>::RM, smem <= kMaxDynSmem ? smem : 0};
+  if constexpr (smem <= kMaxDynSmem) {
+    L.xf_step[prec][F - 1][V] = launch_xf_step<T, N, F, V>;
+  } else {
+    L.xf_step[prec][F - 1][V] = nullptr;
+  }
+}
+
+template <typename T, int N, int V>
+void fill_step_variant(FsLaunchers& L, int prec) {
+  fill_xinv<T, N, V>(L, prec);
+  fill_zz<T, N, 1, V>(L, prec);
+  fill_zz<T, N, 2, V>(L, prec);
+  fill_zz<T, N, 3, V>(L, prec);
+  fill_xf<T, N, 1, V>(L, prec);
+  fill_xf<T, N, 2, V>(L, prec);
+  fill_xf<T, N, 3, V>(L, prec);
+}
+
+template <typename T, int N, int V>
+void clear_step_variant(FsLaunchers& L, int prec) {
+  L.xinv[prec][V] = nullptr;
+  L.xinv_shape[prec][V] = TileShape{XVar<T, N, V>::C, XVar<T, N, V>::RM, 0};
+  for (int f = 0; f < 3; ++f) {
+    L.zz_step[prec][f][V] = nullptr;
+    L.xf_step[prec][f][V] = nullptr;
+    L.zz_shape[prec][f][V] = TileShape{ZVar<V>::P, ZVar<V>::RM, 0};
+    L.xf_shape[prec][f][V] = TileShape{XVar<T, N, V>::C, XVar<T, N, V>::RM, 0};
+  }
+}
+
+template <typename T, int N, int V, bool ON>
+void fill_or_clear(FsLaunchers& L, int prec) {
+  if constexpr (ON) {
+    fill_step_variant<T, N, V>(L, prec);
+  } else {
+    clear_step_variant<T, N, V>(L, prec);
+  }
+}
+
+// The fused-step kernels of one precision, the tile variants in MASK (bit v
+// = variant v).  The double-float kernels are built in the default tile
+// only: they are several times larger to compile than the others.
+template <typename T, int N, int MASK = 0xF>
+void fill_step_kernels(FsLaunchers& L, int prec) {
+  fill_or_clear<T, N, 0, (MASK & 1) != 0>(L, prec);
+  fill_or_clear<T, N, 1, (MASK & 2) != 0>(L, prec);
+  fill_or_clear<T, N, 2, (MASK & 4) != 0>(L, prec);
+  fill_or_clear<T, N, 3, (MASK & 8) != 0>(L, prec);
+}
+
+// The FP64 per-verb kernels.
 template <int N>
-FsLaunchers make_fs_launchers() {
-  FsLaunchers L;
-  L.xinv[0] = launch_xinv<double, N>;
-  L.xinv[1] = launch_xinv<float, N>;
-  L.xinv[2] = launch_xinv<df64, N>;
-  L.zz_step[0][0] = launch_zz_step<double, N, 1>;
-  L.zz_step[0][1] = launch_zz_step<double, N, 2>;
-  L.zz_step[0][2] = launch_zz_step<double, N, 3>;
-  L.zz_step[1][0] = launch_zz_step<float, N, 1>;
-  L.zz_step[1][1] = launch_zz_step<float, N, 2>;
-  L.zz_step[1][2] = launch_zz_step<float, N, 3>;
-  L.zz_step[2][0] = launch_zz_step<df64, N, 1>;
-  L.zz_step[2][1] = launch_zz_step<df64, N, 2>;
-  L.zz_step[2][2] = launch_zz_step<df64, N, 3>;
-  L.xf_step[0][0] = launch_xf_step<double, N, 1>;
-  L.xf_step[0][1] = launch_xf_step<double, N, 2>;
-  L.xf_step[0][2] = launch_xf_step<double, N, 3>;
-  L.xf_step[1][0] = launch_xf_step<float, N, 1>;
-  L.xf_step[1][1] = launch_xf_step<float, N, 2>;
-  L.xf_step[1][2] = launch_xf_step<float, N, 3>;
-  L.xf_step[2][0] = launch_xf_step<df64, N, 1>;
-  L.xf_step[2][1] = launch_xf_step<df64, N, 2>;
-  L.xf_step[2][2] = launch_xf_step<df64, N, 3>;
+void fill_verb_kernels(FsLaunchers& L) {
   L.zinv_phys[0] = launch_zinv_phys<N, 1>;
   L.zinv_phys[1] = launch_zinv_phys<N, 2>;
   L.zfwd_phys = launch_zfwd_phys<N>;
   L.zz_vdn = launch_zz_vdn<N>;
   L.xf_out = launch_xf_out<N>;
-  return L;
 }
 
 // Defined by fs_n<N>.cu; returns nullptr for lengths that are not built.

@@ -22,11 +22,11 @@ from .Timer import Timer
 from .Variable import Variable
 from .Simulation import Simulation
 from .stepper import FieldEquation, Stepper, Term
-from . import equations
+from . import autotune, equations
 
 __all__ = [
     "ArrayFactory", "BasisFunctions", "DataTransferer", "Integrator", "LaplacianSolver", "Parameters",
     "ScalarTracker", "SpatialDifferentiator", "SpectralTransformer", "Ticker", "TimeDerivative", "Timer",
-    "Variable", "Simulation", "FieldEquation", "Stepper", "Term", "equations",
+    "Variable", "Simulation", "FieldEquation", "Stepper", "Term", "autotune", "equations",
     "load_scipy_sparse", "load_scipy_sparse_linalg",
 ]

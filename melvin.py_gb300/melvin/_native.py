@@ -89,6 +89,22 @@ class MgbBatch(C.Structure):
     ]
 
 
+class MgbTileInfo(C.Structure):
+    _fields_ = [
+        ("available", C.c_int32),
+        ("shape", C.c_int32),
+        ("radix", C.c_int32),
+        ("reserved", C.c_int32),
+        ("smem_bytes", C.c_uint64),
+    ]
+
+
+# kernel families of the fused step with tile variants (mgb_family)
+FAMILY_XINV, FAMILY_ZSTEP, FAMILY_XFWD = 0, 1, 2
+FAMILIES = ("xinv", "zstep", "xfwd")
+TILE_VARIANTS = 4
+
+
 class MgbEquation(C.Structure):
     _fields_ = [
         ("nfields", C.c_int32),
@@ -132,6 +148,9 @@ SIGNATURES = {
     "mgb_step_kernel_count": [_P, C.POINTER(MgbEquation), C.POINTER(_I)],
     "mgb_step_events": [_P, C.POINTER(MgbEquation), C.POINTER(_P), C.POINTER(_P), _I, _D, _P, _P, _P,
                         C.POINTER(_P), _I],
+    "mgb_tile_info_get": [_P, _I, _I, _I, C.POINTER(MgbTileInfo)],
+    "mgb_plan_set_tiles": [_P, _I, C.POINTER(_I)],
+    "mgb_plan_get_tiles": [_P, _I, C.POINTER(_I)],
 }
 _RESTYPES = {"mgb_status_string": C.c_char_p, "mgb_last_error": C.c_char_p}
 
@@ -226,6 +245,23 @@ class Plan:
 
     def call(self, name, *args):
         check(getattr(self.lib, name)(self.handle, *args))
+
+    # ---- tile variants of the fused step (fully spectral plans) ----------
+
+    def tile_info(self, family, nfields, variant):
+        """(available, shape, radix, smem_bytes) of one tile variant."""
+        info = MgbTileInfo()
+        self.call("mgb_tile_info_get", int(family), int(nfields), int(variant), C.byref(info))
+        return bool(info.available), info.shape, info.radix, info.smem_bytes
+
+    def get_tiles(self, nfields):
+        t = (_I * 3)()
+        self.call("mgb_plan_get_tiles", int(nfields), t)
+        return tuple(t)
+
+    def set_tiles(self, nfields, tiles):
+        t = (_I * 3)(*[int(v) for v in tiles])
+        self.call("mgb_plan_set_tiles", int(nfields), t)
 
     def __del__(self):
         try:

@@ -120,6 +120,14 @@ class Ensemble:
         self._stepped = True
         return self.diag if diagnostics else None
 
+    def autotune(self, dt, members=None, **kw):
+        """Time the fused step's tile variants on this ensemble (the listed
+        members) and keep the fastest (:func:`melvin.autotune.tune`); the
+        states are left as they were.  Tune before capturing a graph."""
+        from .autotune import tune
+
+        return tune(self, dt=dt, members=members, **kw)
+
     def graph(self, dt, nsteps, members=None):
         """Capture ``nsteps`` steps (a multiple of the integrator order, so
         the history slot pattern repeats) into a CUDA graph; returns a

@@ -111,6 +111,14 @@ class Stepper:
             f.dvar.advance()
         return self.diag if diagnostics else None
 
+    def autotune(self, dt=None, **kw):
+        """Time the fused step's tile variants on this stepper and keep the
+        fastest (:func:`melvin.autotune.tune`); the fields are left as they
+        were."""
+        from .autotune import tune
+
+        return tune(self, dt=dt, **kw)
+
     def kernel_count(self):
         n = C.c_int32()
         N.check(self.plan.lib.mgb_step_kernel_count(self.plan.handle, C.byref(self.eq), C.byref(n)))

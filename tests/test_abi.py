@@ -62,13 +62,18 @@ def test_ctypes_struct_layout_matches_c(tmp_path):
         'printf("%zu %zu %zu %zu\\n", sizeof(mgb_grid), sizeof(mgb_term), sizeof(mgb_field_eq), sizeof(mgb_equation));\n'
         'printf("%zu %zu %zu %zu\\n", offsetof(mgb_grid, lx), offsetof(mgb_grid, precision),'
         " offsetof(mgb_field_eq, terms), offsetof(mgb_equation, f));\n"
+        'printf("%zu %zu %zu %zu %zu\\n", sizeof(mgb_batch), offsetof(mgb_batch, members),'
+        " offsetof(mgb_batch, term_coef), sizeof(mgb_tile_info), offsetof(mgb_tile_info, smem_bytes));\n"
         "return 0;}\n"
     )
     exe = tmp_path / "layout"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     sizes = list(map(int, out[:4]))
-    offs = list(map(int, out[4:]))
+    offs = list(map(int, out[4:8]))
+    more = list(map(int, out[8:]))
     assert sizes == [C.sizeof(N.MgbGrid), C.sizeof(N.MgbTerm), C.sizeof(N.MgbFieldEq), C.sizeof(N.MgbEquation)]
     assert offs == [N.MgbGrid.lx.offset, N.MgbGrid.precision.offset, N.MgbFieldEq.terms.offset,
                     N.MgbEquation.f.offset]
+    assert more == [C.sizeof(N.MgbBatch), N.MgbBatch.members.offset, N.MgbBatch.term_coef.offset,
+                    C.sizeof(N.MgbTileInfo), N.MgbTileInfo.smem_bytes.offset]
