@@ -314,7 +314,7 @@ def run_only(args):
     w0 = workloads.decaying_turbulence(n, n, seed=0)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
     sim, w, dw, step = make_run(n, {"fp64": "double"}.get(args.only, args.only), device, w0)
-    tiles = None if args.no_tune else list(step.autotune().tiles)
+    tiles = _apply_tiles(args, step.plan, 1, lambda: step.autotune())
     for _ in range(args.warmup):
         step.step()
     torch.cuda.synchronize()
@@ -342,6 +342,16 @@ def _timed_run(n, precision, device, w0, steps, warmup, flush, dist, tune=True):
     torch.cuda.synchronize()
     barrier(dist)
     return per_step, per_kernel, (sim, w, dw, step), tuned
+
+
+def _apply_tiles(args, plan, nfields, tune):
+    """--tiles pins the tile variants, --no-tune keeps the defaults,
+    otherwise `tune()` runs the autotuner; returns the selection."""
+    if args.tiles:
+        plan.set_tiles(nfields, [int(v) for v in args.tiles.split(",")])
+    elif not args.no_tune:
+        tune()
+    return list(plan.get_tiles(nfields))
 
 
 def _tiles_summary(plan, tuned):
@@ -509,7 +519,9 @@ def run_ensemble(args):
         w, c = workloads.kelvin_helmholtz(n, n, deltas[b], seed=b)
         ens.load_physical(b, [w, c])
     ens.step(5e-4)
-    tuned = None if args.no_tune else ens.autotune(5e-4)
+    tuned_box = []
+    _apply_tiles(args, ens.plan, 2, lambda: tuned_box.append(ens.autotune(5e-4)))
+    tuned = tuned_box[0] if tuned_box else None
     replay = ens.graph(5e-4, graph_steps)
     for _ in range(max(args.warmup, 1)):
         replay()
@@ -579,6 +591,7 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=2048, help="grid points per side (default 2048)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile variants (no autotuning)")
+    ap.add_argument("--tiles", help="pin the tile variants x-inverse,z,x-forward (e.g. 0,1,1) instead of tuning")
     ap.add_argument("--only", choices=["fp64", "split", "dfloat"],
                     help="run only the timed fused steps of one precision")
     ap.add_argument("--workload", choices=["turbulence", "kh-ensemble", "serving"], default="turbulence",

@@ -129,17 +129,46 @@ __device__ __forceinline__ cx<To> cvt(cx<From> a) {
   return mk(Cvt<To, From>::run(a.x), Cvt<To, From>::run(a.y));
 }
 
-// Shared-memory FFT buffers hold column c of row x at x*CS + c + x/8: one
-// pad element every 8 rows breaks the bank conflicts of the strided Stockham
-// stores (rows 8 apart would otherwise map to the same banks).
-template <int CS>
+// Shared-memory FFT buffers of complex T hold column c of row x at
+// x*CS + c + (x/8)*PAD.  The padding breaks the bank conflicts of the
+// strided Stockham accesses (the first pass stores rows 8 apart; a block
+// transform maps consecutive threads to consecutive columns, then rows).
+// Shared memory serves 8-byte accesses in half-warp phases and 16-byte ones
+// in quarter-warp phases, and the padding that makes consecutive 8-row
+// blocks tile the 32 banks is
+//   16-byte elements: PAD = CS mod 8 (conflict free for every CS);
+//   8-byte elements:  PAD = CS mod 16 for even CS (conflict free), 1 for
+//                     CS = 1 and 0 for other odd CS (about 1.3 wavefronts per
+//                     request either way, so the smaller buffer is kept),
+// found by replaying every pass's addresses against the bank model.  The
+// buffer grows by at most one eighth.
+// A kernel whose other phases access the buffer row by row (a thread per
+// row, as in the z pass) names an explicit stride and pad instead: the
+// layout argument L is then CS + kPadCode * (PAD + 1); a plain column count
+// L < kPadCode takes the rule above.
+template <typename T, int CS>
+struct SmemPad {
+  static constexpr int value =
+      sizeof(cx<T>) >= 16 ? CS % 8 : (CS % 2 == 0 ? CS % 16 : (CS == 1 ? 1 : 0));
+};
+constexpr int kPadCode = 1 << 12;
+template <int CS, int PAD>
+struct ExplicitLayout {
+  static constexpr int value = CS + kPadCode * (PAD + 1);
+};
+template <typename T, int L>
+struct SmemLayout {
+  static constexpr int CS = L % kPadCode;
+  static constexpr int PAD = L / kPadCode ? L / kPadCode - 1 : SmemPad<T, CS>::value;
+};
+template <typename T, int L>
 __host__ __device__ __forceinline__ int sx(int x, int c) {
-  return x * CS + c + (x >> 3);
+  return x * SmemLayout<T, L>::CS + c + (x >> 3) * SmemLayout<T, L>::PAD;
 }
 // Elements of a padded buffer of N rows.
-template <int CS>
+template <typename T, int L>
 __host__ __device__ constexpr int sbuf_elems(int N) {
-  return N * CS + N / 8 + 1;
+  return N * SmemLayout<T, L>::CS + (N / 8) * SmemLayout<T, L>::PAD + 1;
 }
 
 typedef cx<double> zd;

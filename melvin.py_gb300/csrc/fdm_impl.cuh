@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
   const int z0 = blockIdx.x * C;
   const zd* src = (const zd*)maddr(jb.src, a.members, blockIdx.z);
   zd* dout = jb.diff_out.base ? (zd*)maddr(jb.diff_out, a.members, blockIdx.z) : nullptr;
-  for (int e = threadIdx.x; e < sbuf_elems<CP>(N); e += NT) buf[e] = mk<T>(0, 0);
+  for (int e = threadIdx.x; e < sbuf_elems<T, CP>(N); e += NT) buf[e] = mk<T>(0, 0);
   __syncthreads();
   for (int e = threadIdx.x; e < g.nn * CP; e += NT) {
     const int n = e / CP, j = e - n * CP;
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
   for (int e = threadIdx.x; e < N * CP; e += NT) {
     const int x = e / CP, j = e - x * CP;
     const int za = z0 + 2 * j;
-    const cx<T> v = buf[sx<CP>(x, j)];
+    const cx<T> v = buf[sx<T, CP>(x, j)];
     if (za < g.nz) out[(size_t)x * g.nz + za] = v.x;
     if (za + 1 < g.nz) out[(size_t)x * g.nz + za + 1] = v.y;
   }
@@ -419,18 +419,18 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
 #pragma unroll
   for (int f = 0; f < F; ++f) {
     const T* J = (const T*)maddr(a.jin[f], a.members, zm);
-    cx<T>* bf = buf + f * sbuf_elems<CP>(N);
+    cx<T>* bf = buf + f * sbuf_elems<T, CP>(N);
     for (int e = threadIdx.x; e < N * CP; e += NT) {
       const int x = e / CP, j = e - x * CP;
       const int za = z0 + 2 * j;
       const T va = za < g.nz ? J[(size_t)x * g.nz + za] : (T)0;
       const T vb = za + 1 < g.nz ? J[(size_t)x * g.nz + za + 1] : (T)0;
-      bf[sx<CP>(x, j)] = mk(va, vb);
+      bf[sx<T, CP>(x, j)] = mk(va, vb);
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int f = 0; f < F; ++f) block_fft<T, N, CP, CP, NT, -1>(buf + f * sbuf_elems<CP>(N), (const cx<T>*)a.tw);
+  for (int f = 0; f < F; ++f) block_fft<T, N, CP, CP, NT, -1>(buf + f * sbuf_elems<T, CP>(N), (const cx<T>*)a.tw);
   const size_t hslot = (size_t)g.nn * g.nz;
   const int e_bc = g.sdo / 2;
   zd* qf[F];
@@ -464,7 +464,7 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
 #pragma unroll
     for (int f = 0; f < F; ++f) {
       cx<T> A, B;
-      get_pair<T, N, CP>(buf + f * sbuf_elems<CP>(N), j, n, A, B);
+      get_pair<T, N, CP>(buf + f * sbuf_elems<T, CP>(N), j, n, A, B);
       const zd v = cvt<double>(part ? B : A);
       // f = -vec_dot_nabla + linear terms + diffusion (already in the slot)
       zd* hs = hf[f] + (size_t)a.curr * hslot + idx;
@@ -510,7 +510,7 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
 template <typename T, int N>
 cudaError_t launch_fd_xinv(const FdXinvArgs& a, int njobs, int nb, cudaStream_t s) {
   constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
-  const size_t smem = (size_t)sbuf_elems<CP>(N) * sizeof(cx<T>);
+  const size_t smem = (size_t)sbuf_elems<T, CP>(N) * sizeof(cx<T>);
   cudaError_t e = prep_smem(k_fd_xinv<T, N>, smem);
   if (e != cudaSuccess) return e;
   dim3 grid((a.g.nz + C - 1) / C, njobs, nb);
@@ -521,7 +521,7 @@ cudaError_t launch_fd_xinv(const FdXinvArgs& a, int njobs, int nb, cudaStream_t 
 template <typename T, int N, int F>
 cudaError_t launch_fd_xfwd(const FdXfArgs& a, int nb, cudaStream_t s) {
   constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
-  constexpr size_t smem = (size_t)F * sbuf_elems<CP>(N) * sizeof(cx<T>);
+  constexpr size_t smem = (size_t)F * sbuf_elems<T, CP>(N) * sizeof(cx<T>);
   if constexpr (smem > kMaxDynSmem) {
     return cudaErrorInvalidConfiguration;
   } else {

@@ -1,8 +1,8 @@
 // Block-level Stockham FFT held in shared memory.
 //
 // A CTA transforms C interleaved columns of length N (a power of two) that
-// sit in shared memory at buf[sx<CS>(x, c)] (x = position along the
-// transform, c = column, CS >= C the interleave stride, one pad element
+// sit in shared memory at buf[sx<T, CS>(x, c)] (x = position along the
+// transform, c = column, CS >= C the interleave stride, a few pad elements
 // every 8 rows).  Each pass is a radix-8, -4 or
 // -2 butterfly computed in registers: a thread reads all R inputs of its
 // butterflies, the CTA synchronises, and the thread writes the R outputs to
@@ -95,7 +95,7 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, const cx<T>* __restric
     if (NB % NT == 0 || b < NB) {
       const int c = b % C, i = b / C;
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[t][r] = buf[sx<CS>(i + r * (N / R), c)];
+      for (int r = 0; r < R; ++r) v[t][r] = buf[sx<T, CS>(i + r * (N / R), c)];
       if (NS > 1) {
         const int k = i & (NS - 1);
 #pragma unroll
@@ -116,7 +116,7 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, const cx<T>* __restric
       const int k = i & (NS - 1);
       const int base = (i - k) * R + k;
 #pragma unroll
-      for (int r = 0; r < R; ++r) buf[sx<CS>(base + r * NS, c)] = v[t][r];
+      for (int r = 0; r < R; ++r) buf[sx<T, CS>(base + r * NS, c)] = v[t][r];
     }
   }
   __syncthreads();

@@ -155,7 +155,7 @@ struct XinvArgs {
 constexpr int kXLoads = 4;
 
 template <typename T, int N, int C, int RM>
-__global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<C>(N) * sizeof(cx<T>)>::value)) k_xinv(const XinvArgs a) {
+__global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<T, C>(N) * sizeof(cx<T>)>::value)) k_xinv(const XinvArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const GridC& g = a.g;
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<C>(N) * sizeof(cx<T>)>:
   // zero the 2/3-rule gap rows nn+1 .. N-nn-1 (the kept rows are written below)
   for (int e = threadIdx.x; e < (N - g.rows) * C; e += NT) {
     const int x = g.nn + 1 + e / C, c = e % C;
-    buf[sx<C>(x, c)] = mk<T>(0, 0);
+    buf[sx<T, C>(x, c)] = mk<T>(0, 0);
   }
   const int total = g.rows * C;
   for (int e0 = threadIdx.x; e0 < total; e0 += NT * kXLoads) {
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<C>(N) * sizeof(cx<T>)>:
           jb.psi_out[idx] = mk(-(w[u].x * rl), -(w[u].y * rl));
         }
       }
-      buf[sx<C>(row_bin(r, g.nn, N), c)] = v;  // zero for columns past the last mode
+      buf[sx<T, C>(row_bin(r, g.nn, N), c)] = v;  // zero for columns past the last mode
     }
   }
   __syncthreads();
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<C>(N) * sizeof(cx<T>)>:
   cx<T>* out = (cx<T>*)((char*)jb.out + (size_t)blockIdx.z * a.b.inter_stride);
   for (int e = threadIdx.x; e < N * C; e += NT) {
     const int x = e / C, c = e - x * C, m = m0 + c;
-    if (m < g.cols) out[(size_t)x * a.ld + m] = buf[sx<C>(x, c)];
+    if (m < g.cols) out[(size_t)x * a.ld + m] = buf[sx<T, C>(x, c)];
   }
 }
 
@@ -224,16 +224,16 @@ __device__ __forceinline__ void put_pair(cx<T>* buf, int col, int m, cx<T> A, cx
   if (m == 0) {
     buf[col] = mk(A.x, B.x);
   } else {
-    buf[sx<CS>(m, col)] = mk(A.x - B.y, A.y + B.x);
-    buf[sx<CS>(N - m, col)] = mk(A.x + B.y, B.x - A.y);
+    buf[sx<T, CS>(m, col)] = mk(A.x - B.y, A.y + B.x);
+    buf[sx<T, CS>(N - m, col)] = mk(A.x + B.y, B.x - A.y);
   }
 }
 
 // Split the forward transform Z of a + i b into the half spectra of a and b.
 template <typename T, int N, int CS>
 __device__ __forceinline__ void get_pair(const cx<T>* buf, int col, int m, cx<T>& A, cx<T>& B) {
-  const cx<T> zm = buf[sx<CS>(m, col)];
-  const cx<T> zn = buf[sx<CS>((N - m) & (N - 1), col)];
+  const cx<T> zm = buf[sx<T, CS>(m, col)];
+  const cx<T> zn = buf[sx<T, CS>((N - m) & (N - 1), col)];
   const T h = (T)0.5;
   A = mk((zm.x + zn.x) * h, (zm.y - zn.y) * h);
   B = mk((zm.y + zn.y) * h, (zn.x - zm.x) * h);
@@ -244,11 +244,11 @@ __device__ __forceinline__ void get_pair(const cx<T>* buf, int col, int m, cx<T>
 // inv = 1/(2h) (order 2) or 1/(3h) (order 4).
 template <typename T, int N, int CS>
 __device__ __forceinline__ T fd_imag(const cx<T>* buf, int col, int i, int sdo, T inv) {
-  const T p1 = buf[sx<CS>((i + 1) & (N - 1), col)].y;
-  const T m1 = buf[sx<CS>((i - 1) & (N - 1), col)].y;
+  const T p1 = buf[sx<T, CS>((i + 1) & (N - 1), col)].y;
+  const T m1 = buf[sx<T, CS>((i - 1) & (N - 1), col)].y;
   if (sdo == 2) return (p1 - m1) * inv;
-  const T p2 = buf[sx<CS>((i + 2) & (N - 1), col)].y;
-  const T m2 = buf[sx<CS>((i - 2) & (N - 1), col)].y;
+  const T p2 = buf[sx<T, CS>((i + 2) & (N - 1), col)].y;
+  const T m2 = buf[sx<T, CS>((i - 2) & (N - 1), col)].y;
   return (((T)-0.25 * p2 + (T)2 * p1) - (T)2 * m1 + (T)0.25 * m2) * inv;
 }
 
@@ -269,7 +269,7 @@ __device__ __forceinline__ void fd_imag_columns(cx<T>* buf, int sdo, T inv) {
 #pragma unroll
     for (int i = 0; i < EPT; ++i) {
       const int z = threadIdx.x + i * NT;
-      if (z < N) buf[sx<CS>(z, col)].y = v[i];
+      if (z < N) buf[sx<T, CS>(z, col)].y = v[i];
     }
   }
   __syncthreads();
@@ -335,10 +335,33 @@ struct ZzShape {
   static constexpr int CS = P * (NIN > NOUT ? NIN : NOUT);
 };
 
+// Shared-memory layout of the z pass: stride and pad per 8 rows for each
+// element size, field count and row-pair count, chosen with a model of the
+// kernel's shared-memory requests (every FFT pass, the row-per-thread
+// packing, product, stencil and unpacking phases; 8-byte requests served in
+// half-warp phases, 16-byte ones in quarter-warp phases) to minimise the
+// total wavefronts over lengths 256..2048.  Modelled gains over the plain
+// stride with one pad element: 1.0-1.25x with one row pair, up to 3.4x with
+// two or four (an odd stride removes the 8- and 16-way conflicts of the
+// row-per-thread phases).
+template <typename T, int F, int P>
+struct ZzLayout {
+  static constexpr int C0 = ZzShape<F, P>::CS;
+  static constexpr bool wide = sizeof(cx<T>) >= 16;
+  // (F, P) -> stride, pad for 8-byte and 16-byte elements
+  static constexpr int k = (F - 1) * 3 + (P == 1 ? 0 : (P == 2 ? 1 : 2));
+  static constexpr int cs8[9] = {3, 6, 12, 4, 9, 17, 6, 12, 25};
+  static constexpr int pad8[9] = {0, 3, 1, 3, 0, 0, 5, 1, 0};
+  static constexpr int cs16[9] = {3, 6, 13, 5, 9, 17, 6, 13, 25};
+  static constexpr int pad16[9] = {3, 6, 4, 4, 0, 0, 5, 2, 0};
+  static constexpr int value = ExplicitLayout<wide ? cs16[k] : cs8[k], wide ? pad16[k] : pad8[k]>::value;
+  static_assert(SmemLayout<T, value>::CS >= C0, "z-pass stride below the column count");
+};
+
 template <typename T, int N, int F, int P, int RM>
-__global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<ZzShape<F, P>::CS>(N) * sizeof(cx<T>)>::value))
+__global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<T, ZzLayout<T, F, P>::value>(N) * sizeof(cx<T>)>::value))
     k_zz_step(const ZzArgs a) {
-  constexpr int NIN = ZzShape<F, P>::NIN, NOUT = ZzShape<F, P>::NOUT, CS = ZzShape<F, P>::CS;
+  constexpr int NIN = ZzShape<F, P>::NIN, NOUT = ZzShape<F, P>::NOUT, CS = ZzLayout<T, F, P>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const GridC& g = a.g;
@@ -348,7 +371,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<ZzShape<F, P>::CS>(N) *
   // zero the modes nm .. N-nm of the input columns (the rest is written below)
   for (int e = threadIdx.x; e < (N - 2 * nm + 1) * P * NIN; e += NT) {
     const int z = nm + e / (P * NIN), c = e % (P * NIN);
-    buf[sx<CS>(z, c)] = mk<T>(0, 0);
+    buf[sx<T, CS>(z, c)] = mk<T>(0, 0);
   }
   {
     const cx<T>* ux = (const cx<T>*)((const char*)a.in[0] + moff);
@@ -374,7 +397,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<ZzShape<F, P>::CS>(N) *
   for (int z = threadIdx.x; z < N; z += NT) {
     cx<T> w[P * NIN];
 #pragma unroll
-    for (int c = 0; c < P * NIN; ++c) w[c] = buf[sx<CS>(z, c)];
+    for (int c = 0; c < P * NIN; ++c) w[c] = buf[sx<T, CS>(z, c)];
 #pragma unroll
     for (int p = 0; p < P; ++p) {
       const cx<T>* wp = w + p * NIN;
@@ -395,8 +418,8 @@ __global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<ZzShape<F, P>::CS>(N) *
 #pragma unroll
       for (int f = 0; f < F; ++f) {
         const T q0 = wp[2 + f].x, q1 = wp[2 + f].y;
-        buf[sx<CS>(z, p * NOUT + f)] = mk(ux0 * q0, uz0 * q0);
-        buf[sx<CS>(z, p * NOUT + F + f)] = mk(ux1 * q1, uz1 * q1);
+        buf[sx<T, CS>(z, p * NOUT + f)] = mk(ux0 * q0, uz0 * q0);
+        buf[sx<T, CS>(z, p * NOUT + F + f)] = mk(ux1 * q1, uz1 * q1);
       }
     }
   }
@@ -503,7 +526,7 @@ struct XfLoads {
 };
 
 template <typename T, int N, int F, int C, int RM>
-__global__ void __launch_bounds__(NT, (Occ<T, F * sbuf_elems<C>(N) * sizeof(cx<T>)>::value))
+__global__ void __launch_bounds__(NT, (Occ<T, F * sbuf_elems<T, C>(N) * sizeof(cx<T>)>::value))
     k_xf_step(const XfArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
@@ -518,7 +541,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, F * sbuf_elems<C>(N) * sizeof(cx<T
   for (int f = 0; f < F; ++f) {
     const cx<T>* A = (const cx<T>*)((const char*)a.ain[f] + moff);
     const cx<T>* Cc = (const cx<T>*)((const char*)a.cin[f] + moff);
-    cx<T>* bf = buf + f * sbuf_elems<C>(N);
+    cx<T>* bf = buf + f * sbuf_elems<T, C>(N);
     for (int e0 = threadIdx.x; e0 < N * C; e0 += NT * kXLoads) {
       cx<T> p1[kXLoads], m1[kXLoads], p2[kXLoads], m2[kXLoads], cc[kXLoads];
 #pragma unroll
@@ -545,13 +568,13 @@ __global__ void __launch_bounds__(NT, (Occ<T, F * sbuf_elems<C>(N) * sizeof(cx<T
         } else {
           d = (((p2[u] * (T)-0.25 + p1[u] * (T)2) - m1[u] * (T)2) + m2[u] * (T)0.25) * fdx;
         }
-        bf[sx<C>(x, c)] = d + cc[u];  // zero for columns past the last mode
+        bf[sx<T, C>(x, c)] = d + cc[u];  // zero for columns past the last mode
       }
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int f = 0; f < F; ++f) block_fft<T, N, C, C, NT, -1, RM>(buf + f * sbuf_elems<C>(N), (const cx<T>*)a.tw);
+  for (int f = 0; f < F; ++f) block_fft<T, N, C, C, NT, -1, RM>(buf + f * sbuf_elems<T, C>(N), (const cx<T>*)a.tw);
 
   // -1/(nx*nz) is a power of two for the grids built, so scaling in T is exact
   const T neg_norm = (T)(-a.inv_norm);
@@ -603,7 +626,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, F * sbuf_elems<C>(N) * sizeof(cx<T
       for (int f = 0; f < F; ++f) {
         const XfField& eq = a.eq[f];
         // dq[:] = -q.vec_dot_nabla(...) + linear terms
-        const cx<T> J = buf[f * sbuf_elems<C>(N) + sx<C>(k, c)] * neg_norm;
+        const cx<T> J = buf[f * sbuf_elems<T, C>(N) + sx<T, C>(k, c)] * neg_norm;
         zd fv = cvt<double>(J);
         for (int t = 0; t < eq.nterms; ++t) {
           const int sidx = eq.tsrc[t];
@@ -655,7 +678,7 @@ __global__ void __launch_bounds__(NT) k_zinv_phys(const ZinvArgs a) {
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const int x0 = 2 * blockIdx.x;
   const size_t r0 = (size_t)x0 * a.ld, r1 = r0 + a.ld;
-  for (int e = threadIdx.x; e < sbuf_elems<NF>(N); e += NT) buf[e] = mk<T>(0, 0);
+  for (int e = threadIdx.x; e < sbuf_elems<T, NF>(N); e += NT) buf[e] = mk<T>(0, 0);
   __syncthreads();
   for (int m = threadIdx.x; m < a.g.cols; m += NT) {
 #pragma unroll
@@ -669,7 +692,7 @@ __global__ void __launch_bounds__(NT) k_zinv_phys(const ZinvArgs a) {
   for (int z = threadIdx.x; z < N; z += NT) {
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
-      const cx<T> w = buf[sx<NF>(z, f)];
+      const cx<T> w = buf[sx<T, NF>(z, f)];
       a.out[f][(size_t)x0 * N + z] = (double)w.x;
       a.out[f][(size_t)(x0 + 1) * N + z] = (double)w.y;
     }
@@ -690,7 +713,7 @@ __global__ void __launch_bounds__(NT) k_zfwd_phys(const ZfwdArgs a) {
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const int x0 = 2 * blockIdx.x;
   for (int z = threadIdx.x; z < N; z += NT)
-    buf[sx<1>(z, 0)] = mk((T)a.in[(size_t)x0 * N + z], (T)a.in[(size_t)(x0 + 1) * N + z]);
+    buf[sx<T, 1>(z, 0)] = mk((T)a.in[(size_t)x0 * N + z], (T)a.in[(size_t)(x0 + 1) * N + z]);
   __syncthreads();
   block_fft<T, N, 1, 1, NT, -1>(buf, (const cx<T>*)a.tw);
   cx<T>* out = (cx<T>*)a.out;
@@ -724,7 +747,7 @@ __global__ void __launch_bounds__(NT) k_zz_vdn(const ZvdnArgs a) {
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const int x0 = 2 * blockIdx.x;
   const size_t r0 = (size_t)x0 * a.ld, r1 = r0 + a.ld;
-  for (int e = threadIdx.x; e < sbuf_elems<CS>(N); e += NT) buf[e] = mk<T>(0, 0);
+  for (int e = threadIdx.x; e < sbuf_elems<T, CS>(N); e += NT) buf[e] = mk<T>(0, 0);
   __syncthreads();
   const cx<T>* q = (const cx<T>*)a.qin;
   for (int m = threadIdx.x; m < a.g.cols; m += NT) put_pair<T, N, CS>(buf, 0, m, q[r0 + m], q[r1 + m]);
@@ -732,12 +755,12 @@ __global__ void __launch_bounds__(NT) k_zz_vdn(const ZvdnArgs a) {
   block_fft<T, N, 1, CS, NT, +1>(buf, (const cx<T>*)a.tw);
   const size_t p0 = (size_t)x0 * N, p1 = p0 + N;
   for (int z = threadIdx.x; z < N; z += NT) {
-    const cx<T> w = buf[sx<CS>(z, 0)];
+    const cx<T> w = buf[sx<T, CS>(z, 0)];
     const double q0 = (double)w.x, q1 = (double)w.y;
     a.qphys[p0 + z] = q0;
     a.qphys[p1 + z] = q1;
-    buf[sx<CS>(z, 0)] = mk((T)(a.ux[p0 + z] * q0), (T)(a.uz[p0 + z] * q0));
-    buf[sx<CS>(z, 1)] = mk((T)(a.ux[p1 + z] * q1), (T)(a.uz[p1 + z] * q1));
+    buf[sx<T, CS>(z, 0)] = mk((T)(a.ux[p0 + z] * q0), (T)(a.uz[p0 + z] * q0));
+    buf[sx<T, CS>(z, 1)] = mk((T)(a.ux[p1 + z] * q1), (T)(a.uz[p1 + z] * q1));
   }
   __syncthreads();
   fd_imag_columns<T, N, CS, 2>(buf, a.g.sdo, (T)a.fdz);
@@ -779,14 +802,14 @@ __global__ void __launch_bounds__(NT) k_xf_out(const XfOutArgs a) {
     const int x = e / C, c = e - x * C, m = m0 + c;
     cx<T> v = mk<T>(0, 0);
     if (m < g.cols) v = Cc ? jac_x<T, N>(A, Cc, x, m, a.ld, g.sdo, (T)a.fdx) : A[(size_t)x * a.ld + m];
-    buf[sx<C>(x, c)] = v;
+    buf[sx<T, C>(x, c)] = v;
   }
   __syncthreads();
   block_fft<T, N, C, C, NT, -1>(buf, (const cx<T>*)a.tw);
   for (int e = threadIdx.x; e < g.rows * C; e += NT) {
     const int r = e / C, c = e - r * C, m = m0 + c;
     if (m >= g.cols) continue;
-    const cx<T> v = buf[sx<C>(row_bin(r, g.nn, N), c)];
+    const cx<T> v = buf[sx<T, C>(row_bin(r, g.nn, N), c)];
     a.out[(size_t)r * g.cols + m] = mk((double)v.x * a.scale, (double)v.y * a.scale);
   }
 }
@@ -818,7 +841,7 @@ inline cudaError_t prep_smem(K kernel, size_t smem) {
 template <typename T, int N, int V>
 cudaError_t launch_xinv(const XinvArgs& a, int njobs, int nb, cudaStream_t s) {
   constexpr int C = XVar<T, N, V>::C, RM = XVar<T, N, V>::RM;
-  const size_t smem = (size_t)sbuf_elems<C>(N) * sizeof(cx<T>);
+  const size_t smem = (size_t)sbuf_elems<T, C>(N) * sizeof(cx<T>);
   cudaError_t e = prep_smem(k_xinv<T, N, C, RM>, smem);
   if (e != cudaSuccess) return e;
   dim3 grid((a.g.cols + C - 1) / C, njobs, nb);
@@ -829,7 +852,7 @@ cudaError_t launch_xinv(const XinvArgs& a, int njobs, int nb, cudaStream_t s) {
 template <typename T, int N, int F, int V>
 cudaError_t launch_zz_step(const ZzArgs& a, int nb, cudaStream_t s) {
   constexpr int P = ZVar<V>::P, RM = ZVar<V>::RM;
-  const size_t smem = (size_t)sbuf_elems<ZzShape<F, P>::CS>(N) * sizeof(cx<T>);
+  const size_t smem = (size_t)sbuf_elems<T, ZzLayout<T, F, P>::value>(N) * sizeof(cx<T>);
   cudaError_t e = prep_smem(k_zz_step<T, N, F, P, RM>, smem);
   if (e != cudaSuccess) return e;
   k_zz_step<T, N, F, P, RM><<<dim3(a.g.nx / (2 * P), nb), NT, smem, s>>>(a);
@@ -839,7 +862,7 @@ cudaError_t launch_zz_step(const ZzArgs& a, int nb, cudaStream_t s) {
 template <typename T, int N, int F, int V>
 cudaError_t launch_xf_step(const XfArgs& a, int nb, cudaStream_t s) {
   constexpr int C = XVar<T, N, V>::C, RM = XVar<T, N, V>::RM;
-  const size_t smem = (size_t)F * sbuf_elems<C>(N) * sizeof(cx<T>);
+  const size_t smem = (size_t)F * sbuf_elems<T, C>(N) * sizeof(cx<T>);
   cudaError_t e = prep_smem(k_xf_step<T, N, F, C, RM>, smem);
   if (e != cudaSuccess) return e;
   k_xf_step<T, N, F, C, RM><<<dim3((a.g.cols + C - 1) / C, nb), NT, smem, s>>>(a);
@@ -848,7 +871,7 @@ cudaError_t launch_xf_step(const XfArgs& a, int nb, cudaStream_t s) {
 
 template <int N, int NF>
 cudaError_t launch_zinv_phys(const ZinvArgs& a, cudaStream_t s) {
-  const size_t smem = (size_t)sbuf_elems<NF>(N) * sizeof(zd);
+  const size_t smem = (size_t)sbuf_elems<double, NF>(N) * sizeof(zd);
   cudaError_t e = prep_smem(k_zinv_phys<double, N, NF>, smem);
   if (e != cudaSuccess) return e;
   k_zinv_phys<double, N, NF><<<a.g.nx / 2, NT, smem, s>>>(a);
@@ -857,7 +880,7 @@ cudaError_t launch_zinv_phys(const ZinvArgs& a, cudaStream_t s) {
 
 template <int N>
 cudaError_t launch_zfwd_phys(const ZfwdArgs& a, cudaStream_t s) {
-  const size_t smem = (size_t)sbuf_elems<1>(N) * sizeof(zd);
+  const size_t smem = (size_t)sbuf_elems<double, 1>(N) * sizeof(zd);
   cudaError_t e = prep_smem(k_zfwd_phys<double, N>, smem);
   if (e != cudaSuccess) return e;
   k_zfwd_phys<double, N><<<a.g.nx / 2, NT, smem, s>>>(a);
@@ -866,7 +889,7 @@ cudaError_t launch_zfwd_phys(const ZfwdArgs& a, cudaStream_t s) {
 
 template <int N>
 cudaError_t launch_zz_vdn(const ZvdnArgs& a, cudaStream_t s) {
-  const size_t smem = (size_t)sbuf_elems<2>(N) * sizeof(zd);
+  const size_t smem = (size_t)sbuf_elems<double, 2>(N) * sizeof(zd);
   cudaError_t e = prep_smem(k_zz_vdn<double, N>, smem);
   if (e != cudaSuccess) return e;
   k_zz_vdn<double, N><<<a.g.nx / 2, NT, smem, s>>>(a);
@@ -876,7 +899,7 @@ cudaError_t launch_zz_vdn(const ZvdnArgs& a, cudaStream_t s) {
 template <int N>
 cudaError_t launch_xf_out(const XfOutArgs& a, cudaStream_t s) {
   constexpr int C = XTile<double, N>::C;
-  const size_t smem = (size_t)sbuf_elems<C>(N) * sizeof(zd);
+  const size_t smem = (size_t)sbuf_elems<double, C>(N) * sizeof(zd);
   cudaError_t e = prep_smem(k_xf_out<double, N>, smem);
   if (e != cudaSuccess) return e;
   k_xf_out<double, N><<<(a.g.cols + C - 1) / C, NT, smem, s>>>(a);
@@ -910,7 +933,7 @@ struct FsLaunchers {
 template <typename T, int N, int V>
 void fill_xinv(FsLaunchers& L, int prec) {
   constexpr int C = XVar<T, N, V>::C;
-  constexpr size_t smem = (size_t)sbuf_elems<C>(N) * sizeof(cx<T>);
+  constexpr size_t smem = (size_t)sbuf_elems<T, C>(N) * sizeof(cx<T>);
   L.xinv_shape[prec][V] = TileShape{C, XVar<T, N, V>::RM, smem <= kMaxDynSmem ? smem : 0};
   if constexpr (smem <= kMaxDynSmem) {
     L.xinv[prec][V] = launch_xinv<T, N, V>;
@@ -922,7 +945,7 @@ void fill_xinv(FsLaunchers& L, int prec) {
 template <typename T, int N, int F, int V>
 void fill_zz(FsLaunchers& L, int prec) {
   constexpr int P = ZVar<V>::P;
-  constexpr size_t smem = (size_t)sbuf_elems<ZzShape<F, P>::CS>(N) * sizeof(cx<T>);
+  constexpr size_t smem = (size_t)sbuf_elems<T, ZzLayout<T, F, P>::value>(N) * sizeof(cx<T>);
   L.zz_shape[prec][F - 1][V] = TileShape{P, ZVar<V>::RM, smem <= kMaxDynSmem ? smem : 0};
   if constexpr (smem <= kMaxDynSmem) {
     L.zz_step[prec][F - 1][V] = launch_zz_step<T, N, F, V>;
@@ -934,7 +957,7 @@ void fill_zz(FsLaunchers& L, int prec) {
 template <typename T, int N, int F, int V>
 void fill_xf(FsLaunchers& L, int prec) {
   constexpr int C = XVar<T, N, V>::C;
-  constexpr size_t smem = (size_t)F * sbuf_elems<C>(N) * sizeof(cx<T>);
+  constexpr size_t smem = (size_t)F * sbuf_elems<T, C>(N) * sizeof(cx<T>);
   L.xf_shape[prec][F - 1][V] = TileShape{C, XVar<T, N, V>::RM, smem <= kMaxDynSmem ? smem : 0};
   if constexpr (smem <= kMaxDynSmem) {
     L.xf_step[prec][F - 1][V] = launch_xf_step<T, N, F, V>;
