@@ -282,6 +282,73 @@ int mgb_step_events(const mgb_plan* plan, const mgb_equation* eq, void* const* q
                     int32_t curr, double dt, void* work, double* diag, void* stream,
                     void* const* events, int32_t nevents);
 
+/* ---- device-driven run: the Simulation loop without host synchronisation --
+ * The reference keeps t, dt and the loop counter on the host and, in
+ * Simulation.end_loop, fires loop-counted tickers (melvin/Ticker.py:1-35):
+ * the CFL check Integrator.set_dt every cfl_cadence loops
+ * (melvin/Integrator.py:35-44, melvin/Simulation.py:79-84,99-100) and the
+ * scalar trackers every tracker_cadence loops (melvin/Simulation.py:86-97),
+ * and stops when t reaches final_time (melvin/Simulation.py:134-135).  A
+ * driven run keeps all of that in a device-resident mgb_run_state: the
+ * step's kernels read dt from it and return at once for iterations past
+ * the stop point, and a one-thread tick kernel does end_loop, the CFL
+ * shrink / breach test and the tracker samples.  The caller launches
+ * iterations without waiting and reads the state when it wants to.
+ * Loop-counted tickers fire on iterations known in advance, so the caller
+ * passes per iteration which of them fire (MGB_RUN_* flags). */
+typedef enum mgb_run_status {
+  MGB_RUN_RUNNING = 0,
+  MGB_RUN_FINISHED = 1,   /* t reached final_time */
+  MGB_RUN_CFL_BREACH = 2, /* dt > CFL limit or NaN velocity: "CFL condition breached" */
+  MGB_RUN_PAUSED = 3      /* t passed cfg->pause_time: the caller fires its time-based tickers */
+} mgb_run_status;
+
+typedef struct mgb_run_state {   /* device memory, filled by the caller before mgb_run_begin */
+  double t;                /* Simulation._t */
+  double dt;               /* Integrator._dt */
+  int64_t loop;            /* Simulation._loop_counter: completed iterations */
+  int64_t stop_loop;       /* iterations with index >= stop_loop do not run (set on the device) */
+  int64_t cfl_counter;     /* CFL ticker counter: fires after iteration L when counter < L+1 */
+  int64_t tracker_counter; /* tracker ticker counter */
+  int64_t cfl_fired;       /* times the CFL ticker fired */
+  int64_t tracker_fired;   /* times the tracker ticker fired */
+  int32_t status;          /* mgb_run_status */
+  int32_t dt_changed;      /* the last tick shrank dt (coefficients are refreshed) */
+  int32_t ntracked;        /* tracker samples written */
+  int32_t dropped;         /* tracker samples that found the buffer full */
+  double diag[3];          /* kinetic energy, max ux, max uz of the last diagnosed step */
+} mgb_run_state;
+
+typedef struct mgb_run_config {  /* host memory */
+  double final_time;       /* Parameters.final_time */
+  double cfl_cutoff;       /* Parameters.cfl_cutoff */
+  int32_t cfl_cadence;     /* loops between CFL checks */
+  int32_t tracker_cadence; /* loops between tracker samples */
+  int32_t capacity;        /* tracker buffer length */
+  int32_t horizon;         /* the caller ticks at least every `horizon` iterations */
+  double pause_time;       /* pause after the first end_loop with t > pause_time (the next dump or
+                              save time of the time-based tickers; +inf for none) */
+  double* tracker_t;       /* device [capacity]: t of each sample */
+  double* tracker_ke;      /* device [capacity]: kinetic energy (calc_kinetic_energy, melvin/utility.py:42-59) */
+} mgb_run_config;
+
+#define MGB_RUN_TICK 1   /* tick after this iteration (end_loop, stop point) */
+#define MGB_RUN_CFL 2    /* the CFL ticker fires after this iteration (implies a tick) */
+#define MGB_RUN_TRACK 4  /* the tracker ticker fires after this iteration (implies a tick) */
+
+/* Compute the stop point of `state` (device) from its t, dt, loop and
+ * cfg->final_time.  Call after filling the state and after mgb_step_prepare
+ * with the state's dt. */
+int mgb_run_begin(const mgb_plan* plan, mgb_run_state* state, const mgb_run_config* cfg, void* stream);
+/* Iteration `loop` of a driven run: mgb_step with dt read from the state,
+ * skipped on the device when the run stopped before it, then the tick when
+ * `flags` ask for one (after a CFL shrink, the fully spectral update
+ * coefficients are recomputed on the device).  `curr` is the history slot
+ * of this iteration, as for mgb_step. */
+int mgb_run_step(const mgb_plan* plan, const mgb_equation* eq, void* const* q, void* const* hist, int32_t curr,
+                 int64_t loop, int32_t flags, void* work, mgb_run_state* state, const mgb_run_config* cfg,
+                 void* stream);
+
 /* ---- tile variants of the fused step (fully spectral plans) -------------
  * Each of the three fused-step kernels comes in MGB_TILE_VARIANTS variants
  * that differ in the work given to one CTA and in the largest FFT radix:

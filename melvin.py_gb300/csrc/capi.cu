@@ -368,7 +368,7 @@ static int dispatch_step(const mgb_plan* p, const mgb_equation* eq, const StepBa
 }
 
 static int step_impl(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist, int32_t curr,
-                     double dt, void* work, double* diag, void* stream, EventTrack* et) {
+                     double dt, void* work, double* diag, void* stream, EventTrack* et, Gate gate = Gate()) {
   CHECK_PLAN(p);
   CHECK_PTR(eq);
   CHECK_PTR(q);
@@ -390,6 +390,7 @@ static int step_impl(const mgb_plan* p, const mgb_equation* eq, void* const* q, 
   }
   StepBatch sb;
   sb.count = 1;
+  sb.gate = gate;
   for (int f = 0; f < F; ++f) {
     sb.q[f] = (zd*)q[f];
     sb.hist[f] = (zd*)hist[f];
@@ -455,6 +456,7 @@ int mgb_step_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void*
   pr.nfields = F;
   pr.integrator = eq->integrator;
   pr.order = eq->order;
+  pr.driven = false;
   for (int f = 0; f < 3; ++f) pr.kappa[f] = f < F ? eq->f[f].kappa : 0.0;
   return st;
 }
@@ -475,6 +477,60 @@ int mgb_step_events(const mgb_plan* p, const mgb_equation* eq, void* const* q, v
   et.ev = (cudaEvent_t*)events;
   et.nev = nevents;
   return step_impl(p, eq, q, hist, curr, dt, work, diag, stream, &et);
+}
+
+static int check_run_config(const mgb_run_config* cfg, const char* fn) {
+  if (cfg->horizon < 1) return fail(MGB_ERR_INVALID, "%s: horizon=%d (>= 1)", fn, cfg->horizon);
+  if (cfg->cfl_cadence < 0 || cfg->tracker_cadence < 0 || cfg->capacity < 0)
+    return fail(MGB_ERR_INVALID, "%s: negative cadence or capacity", fn);
+  if (cfg->capacity > 0 && (!cfg->tracker_t || !cfg->tracker_ke))
+    return fail(MGB_ERR_INVALID, "%s: tracker buffers missing", fn);
+  return MGB_OK;
+}
+
+int mgb_run_begin(const mgb_plan* p, mgb_run_state* state, const mgb_run_config* cfg, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(state);
+  CHECK_PTR(cfg);
+  if (int st = check_run_config(cfg, __func__)) return st;
+  // no iteration since the last tick: only the stop point is computed
+  return run_tick(p, state, cfg, -1, 0, (cudaStream_t)stream);
+}
+
+int mgb_run_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist, int32_t curr,
+                 int64_t loop, int32_t flags, void* work, mgb_run_state* state, const mgb_run_config* cfg,
+                 void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(eq);
+  CHECK_PTR(state);
+  CHECK_PTR(cfg);
+  if (int st = check_run_config(cfg, __func__)) return st;
+  if (loop < 0) return fail(MGB_ERR_INVALID, "%s: loop=%lld", __func__, (long long)loop);
+  if ((flags & MGB_RUN_CFL) && cfg->cfl_cadence < 1)
+    return fail(MGB_ERR_INVALID, "%s: CFL tick without a CFL cadence", __func__);
+  if ((flags & MGB_RUN_TRACK) && cfg->tracker_cadence < 1)
+    return fail(MGB_ERR_INVALID, "%s: tracker tick without a tracker cadence", __func__);
+  double dt = 0.0;
+  if (!p->g.fdm) {
+    std::lock_guard<std::mutex> lock(p->mu);
+    dt = p->prep.dt;  // the coefficients follow the device dt from here on
+  }
+  Gate gate;
+  gate.stop_at = (const long long*)&state->stop_loop;
+  gate.loop = loop;
+  gate.dt = &state->dt;
+  const bool diagnose = (flags & (MGB_RUN_CFL | MGB_RUN_TRACK)) != 0;
+  int st = step_impl(p, eq, q, hist, curr, dt, work, diagnose ? state->diag : nullptr, stream, nullptr, gate);
+  if (st) return st;
+  if (!p->g.fdm) {
+    std::lock_guard<std::mutex> lock(p->mu);
+    p->prep.driven = true;
+  }
+  if (!flags) return MGB_OK;
+  st = run_tick(p, state, cfg, (long long)loop + 1, flags, (cudaStream_t)stream);
+  if (st) return st;
+  if ((flags & MGB_RUN_CFL) && !p->g.fdm) return fs_prepare(p, eq, dt, work, (cudaStream_t)stream, state);
+  return MGB_OK;
 }
 
 static int check_tile_args(const mgb_plan* p, const char* fn, int32_t nfields) {

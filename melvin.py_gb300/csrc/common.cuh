@@ -173,6 +173,18 @@ __host__ __device__ constexpr int sbuf_elems(int N) {
 
 typedef cx<double> zd;
 
+// Device-side run control of a step launched by the run driver
+// (mgb_run_step): every kernel of the step returns at once when the run
+// stopped before iteration `loop` (CFL breach or final time reached), and
+// the explicit / PECE update of the Dirichlet path reads dt from the run
+// state.  A default Gate (null pointers) is always open.
+struct Gate {
+  const long long* stop_at = nullptr;  // run state: first iteration not to run
+  long long loop = 0;                  // iteration index of this step
+  const double* dt = nullptr;          // run state: current dt
+};
+__device__ __forceinline__ bool gate_closed(const Gate& g) { return g.stop_at != nullptr && g.loop >= *g.stop_at; }
+
 // Which device field a fused kernel reads when it forms a spectral input.
 enum SrcKind : int {
   SRC_COPY = 0,   // the state itself

@@ -90,14 +90,15 @@ inline int grid_for(size_t n) {
   return (int)(b > 152 * 16 ? 152 * 16 : (b < 1 ? 1 : b));
 }
 
-int thomas(const mgb_plan* p, Mptr rhs, double sign, Mptr out, const int* members, int nb, cudaStream_t s) {
+int thomas(const mgb_plan* p, Mptr rhs, double sign, Mptr out, const int* members, int nb, cudaStream_t s,
+           Gate gate) {
   const GridC& g = p->g;
   const size_t smem = (size_t)TH_MODES * g.nz * sizeof(zd);
   if (smem > kMaxDynSmem) return fail(MGB_ERR_UNSUPPORTED, "nz=%d too large for the Thomas kernel", g.nz);
   cudaError_t e = prep_smem(k_thomas, smem);
   if (e != cudaSuccess) return cuda_check(e, "thomas smem");
   k_thomas<<<dim3((g.nn + TH_MODES - 1) / TH_MODES, nb), NT, smem, s>>>(g, rhs, sign, out, members, p->th_inv,
-                                                                        p->th_cp);
+                                                                        p->th_cp, gate);
   MGB_LAUNCH_CHECK();
   return MGB_OK;
 }
@@ -135,7 +136,7 @@ int fd_plan_init(mgb_plan* p) {
 }
 
 int fd_poisson(const mgb_plan* p, const zd* rhs, zd* out, cudaStream_t s) {
-  return thomas(p, mp(rhs), 1.0, mp(out), nullptr, 1, s);
+  return thomas(p, mp(rhs), 1.0, mp(out), nullptr, 1, s, Gate());
 }
 
 int fd_to_physical(const mgb_plan* p, const zd* spec, double* phys, cudaStream_t s) {
@@ -179,7 +180,7 @@ int fd_vec_dot_nabla(const mgb_plan* p, const zd* q, double* q_phys, const doubl
 int fd_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* uz_s, double* psi_phys, double* ux, double* uz,
                 void* work, cudaStream_t s) {
   const GridC& g = p->g;
-  int st = thomas(p, mp(w), -1.0, mp(psi), nullptr, 1, s);
+  int st = thomas(p, mp(w), -1.0, mp(psi), nullptr, 1, s, Gate());
   if (st) return st;
   double* pp = psi_phys ? psi_phys : (double*)work;
   FdXinvArgs xa = {};
@@ -257,10 +258,11 @@ static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, 
     hist[f] = mp(sb.hist[f], hs, 1);
     hslot[f] = mp(sb.hist[f] + (size_t)curr * g.nn * g.nz, hs, 1);
   }
-  int st = thomas(p, qev[0], -1.0, wmp(w, w.psi), sb.members, nb, s);
+  int st = thomas(p, qev[0], -1.0, wmp(w, w.psi), sb.members, nb, s, sb.gate);
   if (st) return st;
   et->mark(s);
   FdXinvArgs xa = {};
+  xa.gate = sb.gate;
   xa.g = g;
   xa.fdz = fd_inv(g.sdo, g.dz);
   xa.tw = twiddles_for(p, false, prec);
@@ -284,6 +286,7 @@ static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, 
   pa.partial = diag ? wmp(w, w.partial) : mp(nullptr);
   pa.fdx = fd_inv(g.sdo, g.dx);
   pa.fdz = fd_inv(g.sdo, g.dz);
+  pa.gate = sb.gate;
   dim3 grid((g.nz + FD_TZ - 1) / FD_TZ, (g.nx + FD_TX - 1) / FD_TX, nb);
   if (prec == MGB_PREC_SPLIT)
     k_fd_phys<float><<<grid, NT, 0, s>>>(pa);
@@ -318,6 +321,7 @@ static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, 
   fa.order = eq->order;
   fa.curr = curr;
   fa.dt = dt;
+  fa.gate = sb.gate;
   fa.inv_nx = 1.0 / (double)g.nx;
   fa.tw = twiddles_for(p, false, prec);
   st = launched(L->xfwd[prec][F - 1](fa, nb, s), "fdm step forward x pass");

@@ -79,7 +79,8 @@ constexpr int TH_MODES = 8;  // modes per CTA
 // Member = blockIdx.y.
 static __global__ void __launch_bounds__(NT) k_thomas(GridC g, Mptr rhs_p, double rhs_sign, Mptr out_p,
                                                const int* members, const double* __restrict__ inv_piv,
-                                               const double* __restrict__ cp) {
+                                               const double* __restrict__ cp, Gate gate) {
+  if (gate_closed(gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   zd* rows = reinterpret_cast<zd*>(smem_raw);  // [TH_MODES][nz]
   const zd* rhs = (const zd*)maddr(rhs_p, members, blockIdx.y);
@@ -156,10 +157,12 @@ struct FdXinvArgs {
   double fdz;    // 1/(2dz) or 1/(3dz)
   const void* tw;
   const int* members;  // member = blockIdx.z
+  Gate gate;
 };
 
 template <typename T, int N>
 __global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
+  if (gate_closed(a.gate)) return;
   constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
@@ -226,6 +229,7 @@ struct FdPhysArgs {
   Mptr partial;      // optional (base null): per-CTA diagnostics (sum ux^2+uz^2, max ux, max uz)
   int nf;
   double fdx, fdz;   // 1/(2dx) or 1/(3dx); same for z
+  Gate gate;
 };
 
 template <typename T>
@@ -238,6 +242,7 @@ __device__ __forceinline__ T st1(T p2, T p1, T m1, T m2, int sdo, T inv) {
 // the outer sdo/2 points of pddz stay 0) (melvin/Variable.py:125-127).
 template <typename T>
 __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
+  if (gate_closed(a.gate)) return;
   constexpr int H = 2;  // storage halo (covers order 4)
   constexpr int SX = FD_TX + 2 * H, SZ = FD_TZ + 2 * H;
   __shared__ T s_ux[SX][FD_TZ];  // x halo
@@ -357,9 +362,10 @@ struct FdXfArgs {
   const int* members;  // member = blockIdx.y
   const double* tcoef; // optional per-slot term coefficients [slot][3][4]
   int nf, mode, order, curr;
-  double dt, inv_nx;
+  double dt, inv_nx;   // dt: used unless gate.dt points at a driven run's dt
   FdXfField eq[3];
   const void* tw;
+  Gate gate;
 };
 
 __device__ __forceinline__ zd fd_ab(const zd* h, size_t slot, int order, int curr, zd f0, double dt) {
@@ -409,6 +415,8 @@ __device__ __forceinline__ zd fd_bc(zd v, int bc, int n, int z, int nz, int e) {
 
 template <typename T, int N, int F>
 __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
+  if (gate_closed(a.gate)) return;
+  const double dt = a.gate.dt ? *a.gate.dt : a.dt;
   constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
@@ -488,10 +496,10 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
       const zd q0 = qf[f][idx];
       zd qn;
       if (a.mode == FD_CORRECT) {
-        const zd am = fd_am(hf[f] + idx, hslot, a.order, a.curr, fv, a.dt);
+        const zd am = fd_am(hf[f] + idx, hslot, a.order, a.curr, fv, dt);
         qn = mk(q0.x + am.x, q0.y + am.y);
       } else {
-        const zd ab = fd_ab(hf[f] + idx, hslot, a.order, a.curr, fv, a.dt);
+        const zd ab = fd_ab(hf[f] + idx, hslot, a.order, a.curr, fv, dt);
         qn = mk(q0.x + ab.x, q0.y + ab.y);
       }
       qn = fd_bc(qn, eq.bc, n, z, g.nz, e_bc);

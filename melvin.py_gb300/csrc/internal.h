@@ -16,6 +16,7 @@ struct PrepRecord {
   double kappa[3] = {0, 0, 0};
   int nfields = 0, integrator = -1, order = 0;
   bool valid = false;
+  bool driven = false;  // a driven run may have refreshed the coefficients for its device dt
 };
 
 struct mgb_plan {
@@ -102,6 +103,7 @@ struct StepBatch {
   zd* hist[3] = {nullptr, nullptr, nullptr};
   size_t q_stride = 0, h_stride = 0;
   const double* tcoef = nullptr;  // optional device [slot][3][4] term coefficients
+  Gate gate;                      // run control (open unless driven by mgb_run_step)
 };
 
 // Shape of tile variant `v` of a fused-step kernel family (fully spectral).
@@ -110,7 +112,11 @@ int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
                   double* diag, cudaStream_t s, EventTrack* et = nullptr);
 size_t fs_step_workspace(const mgb_plan* p, int nfields);
 size_t fs_batch_workspace(const mgb_plan* p, int nfields, int count);
-int fs_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void* work, cudaStream_t s);
+int fs_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void* work, cudaStream_t s,
+               const mgb_run_state* run = nullptr);
+// Tick of a driven run (csrc/driver.cu).
+int run_tick(const mgb_plan* p, mgb_run_state* st, const mgb_run_config* cfg, long long upto, int flags,
+             cudaStream_t s);
 int fs_plan_init(mgb_plan* p);
 
 // ---- Fourier-x / Dirichlet-z family (fdm.cu) ----

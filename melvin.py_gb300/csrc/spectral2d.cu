@@ -209,8 +209,15 @@ size_t fs_batch_workspace(const mgb_plan* p, int nfields, int count) {
 //     a = (1 + (1-alpha) dt L) / (1 - alpha dt L),  b = c_AB / (1 - alpha dt L)
 //   explicit (melvin/Integrator.py:53-56):  a = L,  b = c_AB
 // with c_AB = dt/2 (AB2) or dt/24 (AB4).
+// With `run` set (a driven run), the coefficients follow the run's device
+// dt and are recomputed only after a tick that changed it.
 __global__ void k_update_coefs(GridC g, double kappa, int semi, double dt, double alpha, double cab,
-                               zd* __restrict__ out) {
+                               zd* __restrict__ out, const mgb_run_state* run, int order) {
+  if (run) {
+    if (!run->dt_changed) return;
+    dt = run->dt;
+    cab = order == 2 ? dt / 2 : dt / 24;
+  }
   const size_t total = (size_t)g.rows * g.cols;
   for (size_t i = blockIdx.x * (size_t)NT + threadIdx.x; i < total; i += (size_t)gridDim.x * NT) {
     const int r = (int)(i / g.cols), m = (int)(i - (size_t)r * g.cols);
@@ -226,7 +233,8 @@ __global__ void k_update_coefs(GridC g, double kappa, int semi, double dt, doubl
   }
 }
 
-int fs_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void* work, cudaStream_t s) {
+int fs_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void* work, cudaStream_t s,
+               const mgb_run_state* run) {
   const GridC& g = p->g;
   FsWork w = fs_carve(p, eq->nfields, 1, work);
   const double cab = eq->order == 2 ? dt / 2 : dt / 24;
@@ -235,7 +243,7 @@ int fs_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void* work,
   nb = nb > 152 * 8 ? 152 * 8 : nb;
   for (int f = 0; f < eq->nfields; ++f) {
     k_update_coefs<<<(int)nb, NT, 0, s>>>(g, eq->f[f].kappa, eq->integrator == MGB_INT_SEMI_IMPLICIT ? 1 : 0, dt,
-                                          eq->alpha, cab, w.coef[f]);
+                                          eq->alpha, cab, w.coef[f], run, eq->order);
     MGB_LAUNCH_CHECK();
   }
   return MGB_OK;
@@ -286,7 +294,11 @@ int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
     // the update coefficients in `work` must be the ones for (eq, dt)
     std::lock_guard<std::mutex> lock(p->mu);
     const PrepRecord& pr = p->prep;
-    bool ok = pr.valid && pr.work == work && pr.dt == dt && pr.nfields == F && pr.integrator == eq->integrator &&
+    // a driven step reads dt from the run state (coefficients refreshed on
+    // the device); a plain step needs coefficients prepared for its own dt
+    const bool driven = sb.gate.stop_at != nullptr;
+    bool ok = pr.valid && pr.work == work && (driven || (pr.dt == dt && !pr.driven)) && pr.nfields == F &&
+              pr.integrator == eq->integrator &&
               pr.order == eq->order && (eq->integrator != MGB_INT_SEMI_IMPLICIT || pr.alpha == eq->alpha);
     for (int f = 0; ok && f < F; ++f) ok = pr.kappa[f] == eq->f[f].kappa;
     if (!ok) return fail(MGB_ERR_INVALID, "mgb_step: call mgb_step_prepare for this equation, dt and workspace first");
@@ -305,6 +317,7 @@ int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
   bc.h_stride = sb.h_stride;
   bc.inter_stride = w.inter_stride;
   bc.tcoef = sb.tcoef;
+  bc.gate = sb.gate;
 
   XinvArgs xa = {};
   xa.g = g;

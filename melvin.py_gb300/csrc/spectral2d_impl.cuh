@@ -107,6 +107,7 @@ struct BatchC {
   size_t h_stride;       // zd elements between slots of a history array
   size_t inter_stride;   // bytes between members' intermediate blocks
   const double* tcoef;   // optional per-slot term coefficients [slot][3][4]
+  Gate gate;             // run control of a driven step
 };
 
 __device__ __forceinline__ int batch_slot(const BatchC& b, int z) { return b.members ? b.members[z] : z; }
@@ -156,6 +157,7 @@ constexpr int kXLoads = 4;
 
 template <typename T, int N, int C, int RM>
 __global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<T, C>(N) * sizeof(cx<T>)>::value)) k_xinv(const XinvArgs a) {
+  if (gate_closed(a.b.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const GridC& g = a.g;
@@ -361,6 +363,7 @@ struct ZzLayout {
 template <typename T, int N, int F, int P, int RM>
 __global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<T, ZzLayout<T, F, P>::value>(N) * sizeof(cx<T>)>::value))
     k_zz_step(const ZzArgs a) {
+  if (gate_closed(a.b.gate)) return;
   constexpr int NIN = ZzShape<F, P>::NIN, NOUT = ZzShape<F, P>::NOUT, CS = ZzLayout<T, F, P>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
@@ -528,6 +531,7 @@ struct XfLoads {
 template <typename T, int N, int F, int C, int RM>
 __global__ void __launch_bounds__(NT, (Occ<T, F * sbuf_elems<T, C>(N) * sizeof(cx<T>)>::value))
     k_xf_step(const XfArgs a) {
+  if (gate_closed(a.b.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const GridC& g = a.g;

@@ -99,6 +99,41 @@ class MgbTileInfo(C.Structure):
     ]
 
 
+class MgbRunState(C.Structure):
+    _fields_ = [
+        ("t", C.c_double),
+        ("dt", C.c_double),
+        ("loop", C.c_int64),
+        ("stop_loop", C.c_int64),
+        ("cfl_counter", C.c_int64),
+        ("tracker_counter", C.c_int64),
+        ("cfl_fired", C.c_int64),
+        ("tracker_fired", C.c_int64),
+        ("status", C.c_int32),
+        ("dt_changed", C.c_int32),
+        ("ntracked", C.c_int32),
+        ("dropped", C.c_int32),
+        ("diag", C.c_double * 3),
+    ]
+
+
+class MgbRunConfig(C.Structure):
+    _fields_ = [
+        ("final_time", C.c_double),
+        ("cfl_cutoff", C.c_double),
+        ("cfl_cadence", C.c_int32),
+        ("tracker_cadence", C.c_int32),
+        ("capacity", C.c_int32),
+        ("horizon", C.c_int32),
+        ("pause_time", C.c_double),
+        ("tracker_t", C.c_void_p),
+        ("tracker_ke", C.c_void_p),
+    ]
+
+
+RUN_RUNNING, RUN_FINISHED, RUN_CFL_BREACH, RUN_PAUSED = 0, 1, 2, 3
+RUN_TICK, RUN_CFL, RUN_TRACK = 1, 2, 4
+
 # kernel families of the fused step with tile variants (mgb_family)
 FAMILY_XINV, FAMILY_ZSTEP, FAMILY_XFWD = 0, 1, 2
 FAMILIES = ("xinv", "zstep", "xfwd")
@@ -148,6 +183,9 @@ SIGNATURES = {
     "mgb_step_kernel_count": [_P, C.POINTER(MgbEquation), C.POINTER(_I)],
     "mgb_step_events": [_P, C.POINTER(MgbEquation), C.POINTER(_P), C.POINTER(_P), _I, _D, _P, _P, _P,
                         C.POINTER(_P), _I],
+    "mgb_run_begin": [_P, _P, C.POINTER(MgbRunConfig), _P],
+    "mgb_run_step": [_P, C.POINTER(MgbEquation), C.POINTER(_P), C.POINTER(_P), _I, C.c_int64, _I, _P, _P,
+                     C.POINTER(MgbRunConfig), _P],
     "mgb_tile_info_get": [_P, _I, _I, _I, C.POINTER(MgbTileInfo)],
     "mgb_plan_set_tiles": [_P, _I, C.POINTER(_I)],
     "mgb_plan_get_tiles": [_P, _I, C.POINTER(_I)],
