@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "df64.cuh"
 #include "melvin_gb300.h"
 
@@ -28,6 +30,8 @@ template <typename T>
 __device__ __forceinline__ cx<T> operator-(cx<T> a, cx<T> b) { return mk(a.x - b.x, a.y - b.y); }
 template <typename T>
 __device__ __forceinline__ cx<T> operator*(cx<T> a, T s) { return mk(a.x * s, a.y * s); }
+template <typename T>
+__device__ __forceinline__ cx<T> operator-(cx<T> a) { return mk(-a.x, -a.y); }
 template <typename T>
 __device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) {
   return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);

@@ -93,12 +93,8 @@ inline int grid_for(size_t n) {
 int thomas(const mgb_plan* p, Mptr rhs, double sign, Mptr out, const int* members, int nb, cudaStream_t s,
            Gate gate) {
   const GridC& g = p->g;
-  const size_t smem = (size_t)TH_MODES * g.nz * sizeof(zd);
-  if (smem > kMaxDynSmem) return fail(MGB_ERR_UNSUPPORTED, "nz=%d too large for the Thomas kernel", g.nz);
-  cudaError_t e = prep_smem(k_thomas, smem);
-  if (e != cudaSuccess) return cuda_check(e, "thomas smem");
-  k_thomas<<<dim3((g.nn + TH_MODES - 1) / TH_MODES, nb), NT, smem, s>>>(g, rhs, sign, out, members, p->th_inv,
-                                                                        p->th_cp, gate);
+  k_thomas<<<dim3((g.nn + TH_THREADS - 1) / TH_THREADS, nb), TH_THREADS, 0, s>>>(g, rhs, sign, out, members,
+                                                                              p->th_inv, p->th_cp, gate);
   MGB_LAUNCH_CHECK();
   return MGB_OK;
 }
@@ -186,6 +182,7 @@ int fd_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* uz_s, double* psi_p
   FdXinvArgs xa = {};
   xa.g = g;
   xa.fdz = fd_inv(g.sdo, g.dz);
+  xa.inv_dz2 = 1.0 / (g.dz * g.dz);
   xa.tw = p->tw_x_d;
   xa.job[0] = FdXinvJob{mp(psi), mp(pp), mp(nullptr), 0.0, FD_COPY, nullptr};
   xa.job[1] = FdXinvJob{mp(psi), mp(uz), mp(nullptr), 0.0, FD_UZ, uz_s};
@@ -265,6 +262,7 @@ static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, 
   xa.gate = sb.gate;
   xa.g = g;
   xa.fdz = fd_inv(g.sdo, g.dz);
+  xa.inv_dz2 = 1.0 / (g.dz * g.dz);
   xa.tw = twiddles_for(p, false, prec);
   xa.members = sb.members;
   xa.job[0] = FdXinvJob{wmp(w, w.psi), wmp(w, w.phys[0]), mp(nullptr), 0.0, FD_UX, nullptr};

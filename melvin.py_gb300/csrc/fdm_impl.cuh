@@ -46,10 +46,10 @@ __device__ __forceinline__ char* maddr(const Mptr& p, const int* members, int z)
 inline Mptr mp(const void* base, size_t stride = 0, int by_slot = 0) { return Mptr{(void*)base, stride, by_slot}; }
 
 // pd2dz2 of a complex spectral row at z (interior only), times kappa, plus
-// kappa * d2x n^2 q  ==  kappa * snabla2(q) (melvin/Variable.py:111-113).
-__device__ __forceinline__ zd fd_snabla2(const GridC& g, const zd* row, int n, int z, double kappa) {
+// kappa * d2x n^2 q  ==  kappa * snabla2(q) (melvin/Variable.py:111-113);
+// inv = 1/dz^2, computed once on the host.
+__device__ __forceinline__ zd fd_snabla2(const GridC& g, const zd* row, int n, int z, double kappa, double inv) {
   const int h = g.sdo / 2;
-  const double inv = 1.0 / (g.dz * g.dz);
   double ax = 0, ay = 0;
   if (z >= h && z < g.nz - h) {
     const zd p1 = row[z + 1], c0 = row[z], m1 = row[z - 1];
@@ -70,53 +70,82 @@ __device__ __forceinline__ zd fd_snabla2(const GridC& g, const zd* row, int n, i
 // ---------------------------------------------------------------------------
 // Thomas solve of the per-mode Dirichlet Poisson systems.  The factors
 // (inverse pivots and modified upper diagonal) are precomputed per plan.
-// One thread solves the real or imaginary part of one mode; rows are staged
-// through shared memory so global accesses stay coalesced.
+// One thread solves one mode of one member, its real and imaginary parts as
+// two interleaved dependency chains.  A thread streams its own row in blocks
+// of TH_BLOCK points: the loads of a block are issued before the block's
+// dependent arithmetic, so the chain waits on the FP64 latency only, and a
+// block is a whole 128-byte line of the row.  The forward sweep leaves its
+// result in `out`, which the backward sweep reads back.  `out` may alias
+// the right-hand side: every element is read before it is written.
 // ---------------------------------------------------------------------------
 
-constexpr int TH_MODES = 8;  // modes per CTA
+constexpr int TH_BLOCK = 8;
+constexpr int TH_THREADS = 128;
 
-// Member = blockIdx.y.
-static __global__ void __launch_bounds__(NT) k_thomas(GridC g, Mptr rhs_p, double rhs_sign, Mptr out_p,
-                                               const int* members, const double* __restrict__ inv_piv,
-                                               const double* __restrict__ cp, Gate gate) {
+// Member = blockIdx.y; mode = blockIdx.x * TH_THREADS + threadIdx.x.
+static __global__ void __launch_bounds__(TH_THREADS) k_thomas(GridC g, Mptr rhs_p, double rhs_sign, Mptr out_p,
+                                                      const int* members, const double* __restrict__ inv_piv,
+                                                      const double* __restrict__ cp, Gate gate) {
   if (gate_closed(gate)) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  zd* rows = reinterpret_cast<zd*>(smem_raw);  // [TH_MODES][nz]
-  const zd* rhs = (const zd*)maddr(rhs_p, members, blockIdx.y);
-  zd* out = (zd*)maddr(out_p, members, blockIdx.y);
-  const int n0 = blockIdx.x * TH_MODES;
+  const int n = blockIdx.x * TH_THREADS + threadIdx.x;
+  if (n >= g.nn) return;
   const int nz = g.nz;
-  const int nm = min(TH_MODES, g.nn - n0);
-  for (int e = threadIdx.x; e < nm * nz; e += NT) {
-    const zd v = rhs[(size_t)n0 * nz + e];
-    rows[e] = mk(rhs_sign * v.x, rhs_sign * v.y);
-  }
-  __syncthreads();
-  const int t = threadIdx.x;
-  if (t < 2 * nm) {
-    const int mode = t >> 1, part = t & 1;
-    double* d = reinterpret_cast<double*>(rows + (size_t)mode * nz) + part;  // stride 2 doubles
-    const double* ip = inv_piv + (size_t)(n0 + mode) * nz;
-    const double* c = cp + (size_t)(n0 + mode) * nz;
-    const double a = 1.0 / (g.dz * g.dz);
-    // forward sweep: row 0 and row nz-1 are identity rows
-    double prev = d[0];
-    for (int j = 1; j < nz - 1; ++j) {
-      const double v = (d[2 * j] - a * prev) * ip[j];
-      d[2 * j] = v;
+  const zd* rhs = (const zd*)maddr(rhs_p, members, blockIdx.y) + (size_t)n * nz;
+  zd* out = (zd*)maddr(out_p, members, blockIdx.y) + (size_t)n * nz;
+  const double* ip = inv_piv + (size_t)n * nz;
+  const double* c = cp + (size_t)n * nz;
+  const double a = 1.0 / (g.dz * g.dz);
+  // rhs_sign is +1 or -1, applied as a negation (exact, and no multiply the
+  // compiler could fuse into the sweep's FMA)
+  const bool neg = rhs_sign < 0;
+  // forward sweep: rows 0 and nz-1 are identity rows
+  zd prev = rhs[0];
+  if (neg) prev = mk(-prev.x, -prev.y);
+  out[0] = prev;
+  for (int j0 = 1; j0 < nz - 1; j0 += TH_BLOCK) {
+    zd r[TH_BLOCK];
+    double q[TH_BLOCK];
+#pragma unroll
+    for (int u = 0; u < TH_BLOCK; ++u) {
+      const int j = j0 + u;
+      r[u] = j < nz - 1 ? rhs[j] : mk(0.0, 0.0);
+      q[u] = j < nz - 1 ? ip[j] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < TH_BLOCK; ++u)
+      if (neg) r[u] = mk(-r[u].x, -r[u].y);
+#pragma unroll
+    for (int u = 0; u < TH_BLOCK; ++u) {
+      const int j = j0 + u;
+      if (j >= nz - 1) break;
+      const zd v = mk((r[u].x - a * prev.x) * q[u], (r[u].y - a * prev.y) * q[u]);
+      out[j] = v;
       prev = v;
     }
-    // back substitution
-    double next = d[2 * (nz - 1)];
-    for (int j = nz - 2; j >= 1; --j) {
-      const double v = d[2 * j] - c[j] * next;
-      d[2 * j] = v;
+  }
+  zd last = rhs[nz - 1];
+  if (neg) last = mk(-last.x, -last.y);
+  out[nz - 1] = last;
+  // back substitution
+  zd next = last;
+  for (int j0 = nz - 2; j0 >= 1; j0 -= TH_BLOCK) {
+    zd y[TH_BLOCK];
+    double cc[TH_BLOCK];
+#pragma unroll
+    for (int u = 0; u < TH_BLOCK; ++u) {
+      const int j = j0 - u;
+      y[u] = j >= 1 ? out[j] : mk(0.0, 0.0);
+      cc[u] = j >= 1 ? c[j] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < TH_BLOCK; ++u) {
+      const int j = j0 - u;
+      if (j < 1) break;
+      const zd v = mk(y[u].x - cc[u] * next.x, y[u].y - cc[u] * next.y);
+      out[j] = v;
       next = v;
     }
   }
-  __syncthreads();
-  for (int e = threadIdx.x; e < nm * nz; e += NT) out[(size_t)n0 * nz + e] = rows[e];
 }
 
 // ---------------------------------------------------------------------------
@@ -151,10 +180,42 @@ __device__ __forceinline__ zd fd_ddz_row(const zd* row, int z, int nz, int sdo, 
             (((-0.25 * p2.y + 2 * p1.y) - 2 * m1.y) + 0.25 * m2.y) * inv);
 }
 
+// The same two stencils evaluated in the transform precision T (split and
+// double-float modes: derivatives in the precision of the transforms).
+template <typename T>
+__device__ __forceinline__ cx<T> fd_ddz_row_t(const zd* row, int z, int nz, int sdo, T inv) {
+  const int h = sdo / 2;
+  if (z < h || z >= nz - h) return mk<T>(0, 0);
+  const cx<T> p1 = cvt<T>(row[z + 1]), m1 = cvt<T>(row[z - 1]);
+  if (sdo == 2) return (p1 - m1) * inv;
+  const cx<T> p2 = cvt<T>(row[z + 2]), m2 = cvt<T>(row[z - 2]);
+  return (((p2 * (T)-0.25 + p1 * (T)2) - m1 * (T)2) + m2 * (T)0.25) * inv;
+}
+
+template <typename T>
+__device__ __forceinline__ zd fd_snabla2_t(const GridC& g, const zd* row, int n, int z, T kappa, T inv) {
+  const int h = g.sdo / 2;
+  const cx<T> q = cvt<T>(row[z]);
+  cx<T> acc = mk<T>(0, 0);
+  if (z >= h && z < g.nz - h) {
+    const cx<T> p1 = cvt<T>(row[z + 1]), m1 = cvt<T>(row[z - 1]);
+    if (g.sdo == 2) {
+      acc = ((p1 - q * (T)2) + m1) * inv;
+    } else {
+      const cx<T> p2 = cvt<T>(row[z + 2]), m2 = cvt<T>(row[z - 2]);
+      acc = ((((p2 * (T)(-1.0 / 12) + p1 * (T)(4.0 / 3)) - q * (T)2.5) + m1 * (T)(4.0 / 3)) - m2 * (T)(1.0 / 12)) *
+            inv;
+    }
+  }
+  const T f = (T)g.d2x * (T)(n * n);
+  return cvt<double>((q * f + acc) * kappa);
+}
+
 struct FdXinvArgs {
   GridC g;
   FdXinvJob job[5];
   double fdz;    // 1/(2dz) or 1/(3dz)
+  double inv_dz2;  // 1/dz^2
   const void* tw;
   const int* members;  // member = blockIdx.z
   Gate gate;
@@ -177,29 +238,54 @@ __global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
     const int n = e / CP, j = e - n * CP;
     const int za = z0 + 2 * j, zb = za + 1;
     const zd* row = src + (size_t)n * g.nz;
-    zd A = mk(0.0, 0.0), B = mk(0.0, 0.0);
-    if (jb.kind == FD_UX) {
-      if (za < g.nz) A = fd_ddz_row(row, za, g.nz, g.sdo, a.fdz);
-      if (zb < g.nz) B = fd_ddz_row(row, zb, g.nz, g.sdo, a.fdz);
-      A = mk(-A.x, -A.y);
-      B = mk(-B.x, -B.y);
-    } else {
-      if (za < g.nz) A = row[za];
-      if (zb < g.nz) B = row[zb];
-      if (jb.kind == FD_UZ) {
-        const double b = g.dfx * (double)n;
-        A = mk(-(b * A.y), b * A.x);
-        B = mk(-(b * B.y), b * B.x);
+    if constexpr (std::is_same<T, double>::value) {
+      zd A = mk(0.0, 0.0), B = mk(0.0, 0.0);
+      if (jb.kind == FD_UX) {
+        if (za < g.nz) A = fd_ddz_row(row, za, g.nz, g.sdo, a.fdz);
+        if (zb < g.nz) B = fd_ddz_row(row, zb, g.nz, g.sdo, a.fdz);
+        A = mk(-A.x, -A.y);
+        B = mk(-B.x, -B.y);
+      } else {
+        if (za < g.nz) A = row[za];
+        if (zb < g.nz) B = row[zb];
+        if (jb.kind == FD_UZ) {
+          const double b = g.dfx * (double)n;
+          A = mk(-(b * A.y), b * A.x);
+          B = mk(-(b * B.y), b * B.x);
+        }
       }
-    }
-    if (jb.spec_out) {
-      if (za < g.nz) jb.spec_out[(size_t)n * g.nz + za] = A;
-      if (zb < g.nz) jb.spec_out[(size_t)n * g.nz + zb] = B;
-    }
-    put_pair<T, N, CP>(buf, j, n, cvt<T>(A), cvt<T>(B));
-    if (dout) {
-      if (za < g.nz) dout[(size_t)n * g.nz + za] = fd_snabla2(g, row, n, za, jb.kappa);
-      if (zb < g.nz) dout[(size_t)n * g.nz + zb] = fd_snabla2(g, row, n, zb, jb.kappa);
+      if (jb.spec_out) {
+        if (za < g.nz) jb.spec_out[(size_t)n * g.nz + za] = A;
+        if (zb < g.nz) jb.spec_out[(size_t)n * g.nz + zb] = B;
+      }
+      put_pair<T, N, CP>(buf, j, n, A, B);
+      if (dout) {
+        if (za < g.nz) dout[(size_t)n * g.nz + za] = fd_snabla2(g, row, n, za, jb.kappa, a.inv_dz2);
+        if (zb < g.nz) dout[(size_t)n * g.nz + zb] = fd_snabla2(g, row, n, zb, jb.kappa, a.inv_dz2);
+      }
+    } else {
+      // split / double-float: stencils and the i*kx factor in T, from the
+      // FP64 rows (the per-verb spec_out outputs are FP64-only)
+      cx<T> A = mk<T>(0, 0), B = mk<T>(0, 0);
+      if (jb.kind == FD_UX) {
+        const T inv = (T)a.fdz;
+        if (za < g.nz) A = -fd_ddz_row_t<T>(row, za, g.nz, g.sdo, inv);
+        if (zb < g.nz) B = -fd_ddz_row_t<T>(row, zb, g.nz, g.sdo, inv);
+      } else {
+        if (za < g.nz) A = cvt<T>(row[za]);
+        if (zb < g.nz) B = cvt<T>(row[zb]);
+        if (jb.kind == FD_UZ) {
+          const T b = (T)g.dfx * (T)n;
+          A = mk(-(b * A.y), b * A.x);
+          B = mk(-(b * B.y), b * B.x);
+        }
+      }
+      put_pair<T, N, CP>(buf, j, n, A, B);
+      if (dout) {
+        const T kap = (T)jb.kappa, inv = (T)a.inv_dz2;
+        if (za < g.nz) dout[(size_t)n * g.nz + za] = fd_snabla2_t<T>(g, row, n, za, kap, inv);
+        if (zb < g.nz) dout[(size_t)n * g.nz + zb] = fd_snabla2_t<T>(g, row, n, zb, kap, inv);
+      }
     }
   }
   __syncthreads();
