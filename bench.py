@@ -558,6 +558,73 @@ def run_ensemble(args):
     return 0
 
 
+def run_mixed_ensemble(args):
+    """Kelvin-Helmholtz ensembles of uneven grid sizes in one CUDA graph:
+    64 runs at 128x128, 32 at 256x256, 8 at 512x512 and 2 at 1024x1024
+    (nu = kappa = 1e-4, AB2 semi-implicit, split precision), each size a
+    branch of the graph; against the same ensembles replayed one size after
+    the other."""
+    import numpy as np
+    import torch
+
+    import melvin
+    from melvin import workloads
+    from melvin.ensemble import Ensemble, EnsembleGroup, FieldSpec
+
+    device = torch.device("cuda", dist_env()[2])
+    torch.cuda.set_device(device)
+    sizes = [(128, 64, 1e-3), (256, 32, 5e-4), (512, 8, 2.5e-4), (1024, 2, 1.25e-4)]
+    graph_steps = 8
+    rng = np.random.default_rng(0)
+    ens = []
+    for n, members, dt in sizes:
+        p = melvin.Parameters({"nx": n, "nz": n, "lx": 2 * np.pi, "lz": 2 * np.pi, "final_time": 1.0,
+                               "initial_dt": dt, "precision": args.precision, "device": str(device)})
+        e = Ensemble(p, [FieldSpec(1e-4), FieldSpec(1e-4)], members)
+        for b in range(members):
+            w, c = workloads.kelvin_helmholtz(n, n, float(rng.uniform(0.02, 0.1)), seed=b)
+            e.load_physical(b, [w, c])
+        e.step(dt)
+        if not args.no_tune:
+            e.autotune(dt)
+        ens.append(e)
+    dts = [dt for _, _, dt in sizes]
+    group = EnsembleGroup(ens)
+    together = group.graph(dts, graph_steps)
+    apart = [e.graph(dt, graph_steps) for e, dt in zip(ens, dts)]
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 1)):
+            fn()
+        nrep = max(1, args.steps // graph_steps)
+        ev = []
+        for _ in range(nrep):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            ev.append((e0, e1))
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev) * 1e-3, nrep * graph_steps
+
+    secs, steps = timed(together)
+    secs_apart, _ = timed(lambda: [r() for r in apart])
+    pts = sum(n * n * m for n, m, _ in sizes)
+    print(json.dumps({
+        "workload": "mixed-ensemble", "metric": "Mpts·steps/s (ensembles of uneven sizes, one graph)",
+        "ensembles": [{"grid": f"{n}x{n}", "members": m, "dt": dt} for n, m, dt in sizes],
+        "precision": args.precision, "steps": steps, "graph_steps": graph_steps,
+        "value": round(pts * steps / secs / 1e6, 2), "unit": UNIT,
+        "ms_per_step": round(secs / steps * 1e3, 4),
+        "one_size_after_another": {"value": round(pts * steps / secs_apart / 1e6, 2),
+                                   "ms_per_step": round(secs_apart / steps * 1e3, 4)},
+        "tiles": {f"{e.params.nx}": list(e.plan.get_tiles(2)) for e in ens},
+        "l2": "flushed between graph launches"}), flush=True)
+    return 0
+
+
 def run_serving(args):
     """Poisson stream of double-diffusive convection solves (Fourier-x /
     Dirichlet-z, grids 128x129..1024x1025, R_rho ~ U[1.5, 4], 200..2000
@@ -594,7 +661,8 @@ def main(argv=None):
     ap.add_argument("--tiles", help="pin the tile variants x-inverse,z,x-forward (e.g. 0,1,1) instead of tuning")
     ap.add_argument("--only", choices=["fp64", "split", "dfloat"],
                     help="run only the timed fused steps of one precision")
-    ap.add_argument("--workload", choices=["turbulence", "kh-ensemble", "serving"], default="turbulence",
+    ap.add_argument("--workload", choices=["turbulence", "kh-ensemble", "mixed-ensemble", "serving"],
+                    default="turbulence",
                     help="turbulence: the headline line; kh-ensemble / serving: the batched and serving lines")
     ap.add_argument("--members", type=int, default=256, help="kh-ensemble members")
     ap.add_argument("--requests", type=int, default=200, help="serving requests")
@@ -606,6 +674,8 @@ def main(argv=None):
         return run_reference(args)
     if args.workload == "kh-ensemble":
         return run_ensemble(args)
+    if args.workload == "mixed-ensemble":
+        return run_mixed_ensemble(args)
     if args.workload == "serving":
         return run_serving(args)
     if args.only:

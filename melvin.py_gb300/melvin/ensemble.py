@@ -158,3 +158,74 @@ class Ensemble:
 
         replay.graph = g
         return replay
+
+
+class EnsembleGroup:
+    """Ensembles of different grid sizes (or precisions) advanced together.
+
+    :meth:`graph` captures every ensemble's batched steps into ONE CUDA
+    graph; each ensemble's launch sequence is an independent branch of the
+    graph (forked from and joined back into the capture stream), so the
+    small grids' kernels fill the GPU beside the large ones' and one replay
+    advances every member of every size.  Each ensemble needs its own plan
+    (one ensemble per grid and precision), because a plan's prepared
+    update coefficients belong to one workspace."""
+
+    def __init__(self, ensembles):
+        self.ensembles = list(ensembles)
+        plans = [id(e.plan) for e in self.ensembles]
+        if len(set(plans)) != len(plans):
+            raise ValueError("an EnsembleGroup holds one ensemble per grid and precision")
+        devs = {str(e.device) for e in self.ensembles}
+        if len(devs) != 1:
+            raise ValueError("all ensembles of a group must be on one device")
+        self.device = self.ensembles[0].device
+
+    def _dts(self, dt):
+        return [float(d) for d in (dt if isinstance(dt, (list, tuple)) else [dt] * len(self.ensembles))]
+
+    def step(self, dt, members=None):
+        """One step of every ensemble (launched one ensemble after the other
+        on the current stream); `dt` and `members` may be per-ensemble lists."""
+        mems = members if isinstance(members, (list, tuple)) else [members] * len(self.ensembles)
+        for e, d, m in zip(self.ensembles, self._dts(dt), mems):
+            e.step(d, m)
+
+    def graph(self, dt, nsteps, members=None):
+        """Capture `nsteps` steps of every ensemble (a multiple of every
+        ensemble's integrator order) into one graph; returns a callable that
+        replays it.  dt, member lists and equations are fixed at capture."""
+        dts = self._dts(dt)
+        mems = members if isinstance(members, (list, tuple)) else [members] * len(self.ensembles)
+        for e, d in zip(self.ensembles, dts):
+            if nsteps % e.order:
+                raise ValueError(f"nsteps must be a multiple of every integrator order ({e.order})")
+            if not e._stepped:
+                raise RuntimeError("advance every ensemble once with step() before capturing")
+            e.prepare(d)
+        currs = [e.curr for e in self.ensembles]
+        dev = self.device
+        g = torch.cuda.CUDAGraph()
+        cap = torch.cuda.Stream(device=dev)
+        branches = [torch.cuda.Stream(device=dev) for _ in self.ensembles]
+        cap.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(cap):
+            with torch.cuda.graph(g, stream=cap):
+                for e, d, m, br, c0 in zip(self.ensembles, dts, mems, branches, currs):
+                    br.wait_stream(cap)  # fork
+                    bt = e._batch(m)
+                    for k in range(nsteps):
+                        N.check(e.plan.lib.mgb_batch_step(
+                            e.plan.handle, C.byref(e.eq), C.byref(bt), (c0 + k) % e.order, d, N.ptr(e.work), None,
+                            C.c_void_p(br.cuda_stream)))
+                for br in branches:
+                    cap.wait_stream(br)  # join
+        torch.cuda.current_stream(dev).wait_stream(cap)
+
+        def replay():
+            g.replay()
+            for e, c0 in zip(self.ensembles, currs):
+                e.curr = c0  # nsteps is a multiple of every order
+
+        replay.graph = g
+        return replay

@@ -141,3 +141,57 @@ def test_per_slot_term_coefficients(cuda):
             ref.step()
         for f in range(3):
             assert rel_l2(ens.q[k, f].cpu().numpy(), ref.q[f]) < TOL, (k, f)
+
+
+def _mixed_group(seed_shift=0):
+    import melvin
+    from melvin import _native as N
+    from melvin.ensemble import Ensemble, EnsembleGroup, FieldSpec
+
+    out = []
+    for n, nb in ((64, 3), (128, 2)):
+        g = O.Grid(n, n, 2 * np.pi, 2 * np.pi)
+        ens = Ensemble(kh_params(n, n, "split"), [FieldSpec(1e-3), FieldSpec(2e-3)], nb)
+        for b in range(nb):
+            ens.load_physical(b, list(P.kh_ic(g, 0.2 + 0.05 * b, seed=b + seed_shift)))
+        out.append(ens)
+    p = melvin.Parameters({"nx": 64, "nz": 65, "lx": 2.0, "lz": 1.0, "final_time": 1.0, "initial_dt": 1e-6,
+                           "discretisation": ["spectral", "fdm"], "integrator": "explicit", "precision": "split",
+                           "device": "cuda:0"})
+    Pr, RaT = 7.0, 1e5
+    fields = [FieldSpec(Pr, [(1, "ddx", -Pr * RaT), (2, "ddx", Pr * RaT / 2.0)], N.BC_DIRICHLET_W),
+              FieldSpec(1.0, [], N.BC_DIRICHLET_T), FieldSpec(0.01, [], N.BC_DIRICHLET_T)]
+    ddc = Ensemble(p, fields, 2)
+    from melvin.workloads import conductive
+    for b in range(2):
+        ddc.load_physical(b, [np.zeros((64, 65)), conductive(64, 65, 2.0, 1.0, seed=b), conductive(64, 65, 2.0, 1.0,
+                                                                                                   seed=9 + b)])
+    out.append(ddc)
+    return EnsembleGroup(out), [5e-3, 5e-3, 1e-6]
+
+
+def test_group_graph_equals_individual_steps(cuda):
+    grp_a, dts = _mixed_group()
+    for e, d in zip(grp_a.ensembles, dts):
+        e.step(d)
+    replay = grp_a.graph(dts, 4)
+    replay()
+    replay()
+    grp_b, _ = _mixed_group()
+    for e, d in zip(grp_b.ensembles, dts):
+        for _ in range(9):
+            e.step(d)
+    torch.cuda.synchronize()
+    for ea, eb in zip(grp_a.ensembles, grp_b.ensembles):
+        assert ea.curr == eb.curr
+        assert torch.equal(ea.q, eb.q)
+        assert torch.equal(ea.hist, eb.hist)
+
+
+def test_group_rejects_shared_plans(cuda):
+    from melvin.ensemble import Ensemble, EnsembleGroup, FieldSpec
+
+    a = Ensemble(kh_params(64, 64), [FieldSpec(1e-3)], 2)
+    b = Ensemble(kh_params(64, 64), [FieldSpec(1e-3)], 3)
+    with pytest.raises(ValueError):
+        EnsembleGroup([a, b])
