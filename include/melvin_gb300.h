@@ -93,6 +93,38 @@ int mgb_to_physical(const mgb_plan* plan, const void* spec, double* phys, void* 
 /* Physical -> spectral: SpectralTransformer.to_spectral (:152-199, :63-88). */
 int mgb_to_spectral(const mgb_plan* plan, const double* phys, void* spec, void* work, void* stream);
 
+/* ---- cosine and sine bases ---------------------------------------------
+ * Basis functions per axis (melvin/BasisFunctions.py:5-9).  The reference
+ * transforms a cosine or sine axis of n points as a mirrored periodic signal
+ * of 2(n-1) points (melvin/SpectralTransformer.py:90-199); here that length
+ * must be a power of two in [16, 4096], i.e. n = 2^k + 1, and a plan accepts
+ * such an axis (complex-exponential verbs then return MGB_ERR_UNSUPPORTED).
+ * Unlike the reference, to_physical leaves its input unchanged (the
+ * reference doubles the zeroth cosine mode of its input in place,
+ * melvin/SpectralTransformer.py:122-125; the result equals the reference's
+ * first call).  Fully spectral plans only. */
+typedef enum mgb_basis {
+  MGB_BASIS_COMPLEX_EXP = 0,
+  MGB_BASIS_COSINE = 1,
+  MGB_BASIS_SINE = 2
+} mgb_basis;
+
+/* SpectralTransformer.to_physical / to_spectral with basis (bx, bz). */
+int mgb_to_physical_basis(const mgb_plan* plan, int32_t bx, int32_t bz, const void* spec, double* phys, void* work,
+                          void* stream);
+int mgb_to_spectral_basis(const mgb_plan* plan, int32_t bx, int32_t bz, const double* phys, void* spec, void* work,
+                          void* stream);
+/* Spectral derivative verbs with the basis factors of gen_diff_factors /
+ * gen_diff2_factors (melvin/BasisFunctions.py:44-59,
+ * melvin/SpatialDifferentiator.py:50-74): cosine and sine axes multiply by
+ * the real -pi n/L or pi n/L, and by -(pi n/L)^2 for second derivatives. */
+int mgb_spectral_derivative_basis(const mgb_plan* plan, int32_t kind, int32_t bx, int32_t bz, const void* in,
+                                  void* out, void* stream);
+/* calc_lap(basis_fns) (melvin/SpatialDifferentiator.py:70-74). */
+int mgb_laplacian_basis(const mgb_plan* plan, int32_t bx, int32_t bz, double* lap, void* stream);
+/* The fully spectral Poisson divide with that Laplacian (melvin/LaplacianSolver.py:58-68). */
+int mgb_poisson_solve_basis(const mgb_plan* plan, int32_t bx, int32_t bz, const void* rhs, void* out, void* stream);
+
 /* ---- derivatives (melvin/SpatialDifferentiator.py) ---------------------- */
 
 /* Central finite-difference d/dx of a physical field, x periodic

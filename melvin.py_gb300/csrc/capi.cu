@@ -96,6 +96,7 @@ static int upload_twiddles(int n, void** td, void** tf, void** tdf) {
 
 static void release(mgb_plan* p) {
   if (!p) return;
+  for (auto& kv : p->tw_extra) cudaFree(kv.second);
   cudaFree(p->tw_x_d);
   cudaFree(p->tw_x_f);
   cudaFree(p->tw_x_df);
@@ -109,6 +110,35 @@ static void release(mgb_plan* p) {
   cudaFree(p->tab_f);
   delete p;
 }
+
+const void* mirror_twiddles(const mgb_plan* p, int L) {
+  if (L == p->g.nx && p->tw_x_d) return p->tw_x_d;
+  if (!p->g.fdm && L == p->g.nz && p->tw_z_d) return p->tw_z_d;
+  std::lock_guard<std::mutex> lock(p->mu);
+  auto it = p->tw_extra.find(L);
+  if (it != p->tw_extra.end()) return it->second;
+  void *td = nullptr, *tf = nullptr, *tdf = nullptr;
+  const int st = upload_twiddles(L, &td, &tf, &tdf);
+  cudaFree(tf);
+  cudaFree(tdf);
+  if (st != MGB_OK) {
+    cudaFree(td);
+    return nullptr;
+  }
+  p->tw_extra[L] = td;
+  return td;
+}
+
+int need_exp_ffts(const mgb_plan* p, const char* fn) {
+  if (p->exp_ok) return MGB_OK;
+  return fail(MGB_ERR_UNSUPPORTED,
+              "%s: complex-exponential transforms need power-of-two nx and nz; this plan has an axis of 2^k+1 "
+              "points, which only the cosine and sine bases use", fn);
+}
+
+// An axis of n points that a cosine or sine basis turns into a power-of-two
+// transform of 2(n-1) points.
+static bool mirrored_len(int n) { return n > 2 && pow2_in_range(2 * (n - 1)); }
 
 }  // namespace mgb
 
@@ -141,10 +171,15 @@ int mgb_plan_create(const mgb_grid* grid, mgb_plan** out) {
   CHECK_PTR(out);
   *out = nullptr;
   const mgb_grid& G = *grid;
-  if (!pow2_in_range(G.nx))
-    return fail(MGB_ERR_UNSUPPORTED, "nx=%d: x transforms need a power of two in [16, 4096]", G.nx);
-  if (!G.fdm_z && !pow2_in_range(G.nz))
-    return fail(MGB_ERR_UNSUPPORTED, "nz=%d: fully spectral z transforms need a power of two in [16, 4096]", G.nz);
+  const bool px = pow2_in_range(G.nx), pz = pow2_in_range(G.nz);
+  if (!px && (G.fdm_z || !mirrored_len(G.nx)))
+    return fail(MGB_ERR_UNSUPPORTED,
+                "nx=%d: x transforms need a power of two in [16, 4096] (or 2^k+1 points with a cosine or sine "
+                "basis on a fully spectral grid)", G.nx);
+  if (!G.fdm_z && !pz && !mirrored_len(G.nz))
+    return fail(MGB_ERR_UNSUPPORTED,
+                "nz=%d: fully spectral z transforms need a power of two in [16, 4096] (or 2^k+1 points with a "
+                "cosine or sine basis)", G.nz);
   if (G.fdm_z && (G.nz < 5 || G.nz > 1800))
     return fail(MGB_ERR_UNSUPPORTED, "nz=%d: FDM z axis needs 5 <= nz <= 1800", G.nz);
   if (G.sdo != 2 && G.sdo != 4)
@@ -172,8 +207,9 @@ int mgb_plan_create(const mgb_grid* grid, mgb_plan** out) {
   g.d2x = -((tp * tp) / (G.lx * G.lx));
   g.d2z = -((tp * tp) / (G.lz * G.lz));
   cudaGetDevice(&p->device);
-  int st = upload_twiddles(G.nx, &p->tw_x_d, &p->tw_x_f, &p->tw_x_df);
-  if (!st && !G.fdm_z) st = upload_twiddles(G.nz, &p->tw_z_d, &p->tw_z_f, &p->tw_z_df);
+  p->exp_ok = px && (G.fdm_z || pz);
+  int st = px ? upload_twiddles(G.nx, &p->tw_x_d, &p->tw_x_f, &p->tw_x_df) : MGB_OK;
+  if (!st && !G.fdm_z && pz) st = upload_twiddles(G.nz, &p->tw_z_d, &p->tw_z_f, &p->tw_z_df);
   if (!st && !G.fdm_z) st = fs_plan_init(p);
   if (!st && G.fdm_z) st = fd_plan_init(p);
   if (st) {
@@ -218,6 +254,7 @@ int mgb_workspace_bytes(const mgb_plan* p, int32_t family, int32_t nfields, size
 
 int mgb_to_physical(const mgb_plan* p, const void* spec, double* phys, void* work, void* stream) {
   CHECK_PLAN(p);
+  if (int st = need_exp_ffts(p, __func__)) return st;
   CHECK_PTR(spec);
   CHECK_PTR(phys);
   if (p->g.fdm) return fd_to_physical(p, (const zd*)spec, phys, (cudaStream_t)stream);
@@ -227,11 +264,53 @@ int mgb_to_physical(const mgb_plan* p, const void* spec, double* phys, void* wor
 
 int mgb_to_spectral(const mgb_plan* p, const double* phys, void* spec, void* work, void* stream) {
   CHECK_PLAN(p);
+  if (int st = need_exp_ffts(p, __func__)) return st;
   CHECK_PTR(spec);
   CHECK_PTR(phys);
   if (p->g.fdm) return fd_to_spectral(p, phys, (zd*)spec, (cudaStream_t)stream);
   CHECK_PTR(work);
   return fs_to_spectral(p, phys, (zd*)spec, work, (cudaStream_t)stream);
+}
+
+int mgb_to_physical_basis(const mgb_plan* p, int32_t bx, int32_t bz, const void* spec, double* phys, void* work,
+                          void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(spec);
+  CHECK_PTR(phys);
+  CHECK_PTR(work);
+  if (bx == MGB_BASIS_COMPLEX_EXP && bz == MGB_BASIS_COMPLEX_EXP) return mgb_to_physical(p, spec, phys, work, stream);
+  return mirror_to_physical(p, bx, bz, (const zd*)spec, phys, work, (cudaStream_t)stream);
+}
+
+int mgb_to_spectral_basis(const mgb_plan* p, int32_t bx, int32_t bz, const double* phys, void* spec, void* work,
+                          void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(spec);
+  CHECK_PTR(phys);
+  CHECK_PTR(work);
+  if (bx == MGB_BASIS_COMPLEX_EXP && bz == MGB_BASIS_COMPLEX_EXP) return mgb_to_spectral(p, phys, spec, work, stream);
+  return mirror_to_spectral(p, bx, bz, phys, (zd*)spec, work, (cudaStream_t)stream);
+}
+
+int mgb_spectral_derivative_basis(const mgb_plan* p, int32_t kind, int32_t bx, int32_t bz, const void* in, void* out,
+                                  void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(in);
+  CHECK_PTR(out);
+  return pw_spectral_derivative_basis(p, kind, bx, bz, (const zd*)in, (zd*)out, (cudaStream_t)stream);
+}
+
+int mgb_laplacian_basis(const mgb_plan* p, int32_t bx, int32_t bz, double* lap, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(lap);
+  return pw_laplacian_basis(p, bx, bz, lap, (cudaStream_t)stream);
+}
+
+int mgb_poisson_solve_basis(const mgb_plan* p, int32_t bx, int32_t bz, const void* rhs, void* out, void* stream) {
+  CHECK_PLAN(p);
+  CHECK_PTR(rhs);
+  CHECK_PTR(out);
+  return pw_poisson_basis(p, bx, bz, (const zd*)rhs, (zd*)out, (cudaStream_t)stream);
 }
 
 int mgb_pddx(const mgb_plan* p, const double* in, double* out, void* stream) {
@@ -274,6 +353,7 @@ int mgb_poisson_solve(const mgb_plan* p, const void* rhs, void* out, void* strea
 int mgb_vec_dot_nabla(const mgb_plan* p, const void* q_spec, double* q_phys, const double* ux, const double* uz,
                       void* out_spec, void* work, void* stream) {
   CHECK_PLAN(p);
+  if (int st = need_exp_ffts(p, __func__)) return st;
   CHECK_PTR(q_spec);
   CHECK_PTR(q_phys);
   CHECK_PTR(ux);
@@ -288,6 +368,7 @@ int mgb_vec_dot_nabla(const mgb_plan* p, const void* q_spec, double* q_phys, con
 int mgb_velocity_from_vorticity(const mgb_plan* p, const void* w_spec, void* psi_spec, void* ux_spec, void* uz_spec,
                                 double* psi_phys, double* ux_phys, double* uz_phys, void* work, void* stream) {
   CHECK_PLAN(p);
+  if (int st = need_exp_ffts(p, __func__)) return st;
   CHECK_PTR(w_spec);
   CHECK_PTR(psi_spec);
   CHECK_PTR(ux_phys);
@@ -361,6 +442,7 @@ static int check_equation(const mgb_equation* eq, int32_t curr) {
 
 static int dispatch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb, int32_t curr, double dt,
                          void* work, double* diag, void* stream, EventTrack* et) {
+  if (int st = need_exp_ffts(p, "mgb_step")) return st;
   if (p->g.fdm) return fd_batch_step(p, eq, sb, curr, dt, work, diag, (cudaStream_t)stream, et);
   if (eq->integrator != MGB_INT_SEMI_IMPLICIT && eq->integrator != MGB_INT_EXPLICIT)
     return fail(MGB_ERR_UNSUPPORTED, "fully spectral step: integrator %d", eq->integrator);
@@ -535,6 +617,7 @@ int mgb_run_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void
 
 static int check_tile_args(const mgb_plan* p, const char* fn, int32_t nfields) {
   if (p->g.fdm) return fail(MGB_ERR_UNSUPPORTED, "%s: tile variants exist for fully spectral plans only", fn);
+  if (int st = need_exp_ffts(p, fn)) return st;
   if (nfields < 1 || nfields > 3) return fail(MGB_ERR_INVALID, "%s: nfields=%d outside 1..3", fn, nfields);
   return MGB_OK;
 }

@@ -207,6 +207,10 @@ struct GridC {
   double dx, dz;
   double dfx, dfz;  // 2*pi/lx, 2*pi/lz (imaginary part of the derivative factor)
   double d2x, d2z;  // -(2*pi)^2/lx^2, -(2*pi)^2/lz^2
+  // Basis of each axis for the spectral derivative verbs: 0 complex
+  // exponential (factor i*dfx*n), 1 cosine / 2 sine (real factor dfx*n, with
+  // dfx = -pi/lx or pi/lx and d2x = -pi^2/lx^2, melvin/BasisFunctions.py:26-59).
+  int bx = 0, bz = 0;
 };
 
 // Spectral row r of the (2nn+1)-row block -> signed mode number n.

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <map>
 #include <mutex>
 
 #include "common.cuh"
@@ -40,6 +41,13 @@ struct mgb_plan {
   float* tab_f = nullptr;
   void* tab_df = nullptr;  // tux, tuz as double-float
   int device = 0;
+  // Both axes are power-of-two lengths, so complex-exponential transforms
+  // (every verb except the cosine/sine ones) can run.  An axis of 2^k + 1
+  // points is usable with cosine and sine bases only.
+  bool exp_ok = true;
+  // Twiddle tables of other transform lengths (cosine/sine bases), by length
+  // (guarded by mu).
+  mutable std::map<int, void*> tw_extra;
   // Fused-step tile variants [nfields-1][mgb_family] (guarded by mu).
   int tiles[3][3] = {};
   mutable std::mutex mu;
@@ -105,6 +113,20 @@ struct StepBatch {
   const double* tcoef = nullptr;  // optional device [slot][3][4] term coefficients
   Gate gate;                      // run control (open unless driven by mgb_run_step)
 };
+
+// Twiddles exp(-2 pi i t/L) in double for transform length L (the plan's own
+// tables, or one made on first use); null when it cannot be made.
+const void* mirror_twiddles(const mgb_plan* p, int L);
+// Cosine/sine-basis transforms (csrc/mirror.cu); basis 0 exp, 1 cosine, 2 sine.
+int mirror_to_physical(const mgb_plan* p, int bx, int bz, const zd* spec, double* phys, void* work, cudaStream_t s);
+int mirror_to_spectral(const mgb_plan* p, int bx, int bz, const double* phys, zd* spec, void* work, cudaStream_t s);
+int basis_length(int basis, int n);
+// Pointwise spectral verbs with per-axis bases (csrc/pointwise.cu).
+int pw_spectral_derivative_basis(const mgb_plan* p, int kind, int bx, int bz, const zd* in, zd* out, cudaStream_t s);
+int pw_laplacian_basis(const mgb_plan* p, int bx, int bz, double* lap, cudaStream_t s);
+int pw_poisson_basis(const mgb_plan* p, int bx, int bz, const zd* rhs, zd* out, cudaStream_t s);
+// MGB_ERR_UNSUPPORTED unless both axes can take complex-exponential FFTs.
+int need_exp_ffts(const mgb_plan* p, const char* fn);
 
 // Shape of tile variant `v` of a fused-step kernel family (fully spectral).
 int fs_tile_info(const mgb_plan* p, int family, int nfields, int v, mgb_tile_info* out);

@@ -55,6 +55,7 @@ extern "C" int mgb_vec_dot_nabla_noalloc(const mgb_plan* p, const void* q_spec, 
                                          const double* uz, void* out_spec, void* stream) {
   if (!p) return fail(MGB_ERR_INVALID, "%s: null plan", __func__);
   if (!q_spec || !q_phys || !ux || !uz || !out_spec) return fail(MGB_ERR_INVALID, "%s: null array", __func__);
+  if (int st = need_exp_ffts(p, __func__)) return st;
   const GridC& g = p->g;
   // scratch: two x-pass intermediates (fully spectral) or one physical field (FDM z)
   const size_t need = g.fdm ? (size_t)g.nx * g.nz * sizeof(double) : 2 * inter_bytes(g, MGB_PREC_DOUBLE);

@@ -1,6 +1,8 @@
 // Pointwise and stencil kernels of the per-verb API: physical finite
 // differences, spectral derivative verbs, the spectral Poisson divide, the
 // Adams-Bashforth/Moulton updates and the diagnostic reductions.
+#include <math.h>
+
 #include "internal.h"
 
 namespace mgb {
@@ -105,7 +107,7 @@ __global__ void k_spec_deriv(GridC g, int kind, const zd* __restrict__ in, zd* _
     zd o = mk(0.0, 0.0);
     if (kind == MGB_DDX) {
       const double b = g.dfx * (double)n;
-      o = mk(-(b * v.y), b * v.x);
+      o = g.bx ? mk(b * v.x, b * v.y) : mk(-(b * v.y), b * v.x);
     } else if (kind == MGB_DDZ) {
       if (g.fdm) {
         bool inside;
@@ -114,7 +116,7 @@ __global__ void k_spec_deriv(GridC g, int kind, const zd* __restrict__ in, zd* _
         o = inside ? mk(d.x, d.y) : mk(0.0, 0.0);
       } else {
         const double b = g.dfz * (double)m;
-        o = mk(-(b * v.y), b * v.x);
+        o = g.bz ? mk(b * v.x, b * v.y) : mk(-(b * v.y), b * v.x);
       }
     } else {
       zd dx2 = mk(0.0, 0.0), dz2 = mk(0.0, 0.0);
@@ -325,6 +327,55 @@ int pw_laplacian(const mgb_plan* p, double* lap, cudaStream_t s) {
 
 int pw_poisson_spectral(const mgb_plan* p, const zd* rhs, zd* out, cudaStream_t s) {
   const GridC& g = p->g;
+  k_poisson_spectral<<<nblocks((size_t)g.rows * g.cols), PT, 0, s>>>(g, rhs, out);
+  MGB_LAUNCH_CHECK();
+  return MGB_OK;
+}
+
+// The plan's grid constants with the derivative factors of bases (bx, bz)
+// (melvin/BasisFunctions.py:26-59): cosine -pi/L, sine pi/L (real), second
+// derivative -pi^2/L^2.
+static int basis_grid(const mgb_plan* p, int bx, int bz, GridC& g, const char* fn) {
+  g = p->g;
+  if (bx < 0 || bx > 2 || bz < 0 || bz > 2) return fail(MGB_ERR_INVALID, "%s: basis (%d, %d)", fn, bx, bz);
+  if (g.fdm && (bx || bz)) return fail(MGB_ERR_UNSUPPORTED, "%s: cosine and sine bases need a fully spectral grid", fn);
+  const double pi = M_PI;
+  if (bx) {
+    g.bx = bx;
+    g.dfx = (bx == MGB_BASIS_SINE ? pi : -pi) / p->grid.lx;
+    g.d2x = -((pi * pi) / (p->grid.lx * p->grid.lx));
+  }
+  if (bz) {
+    g.bz = bz;
+    g.dfz = (bz == MGB_BASIS_SINE ? pi : -pi) / p->grid.lz;
+    g.d2z = -((pi * pi) / (p->grid.lz * p->grid.lz));
+  }
+  return MGB_OK;
+}
+
+int pw_spectral_derivative_basis(const mgb_plan* p, int kind, int bx, int bz, const zd* in, zd* out, cudaStream_t s) {
+  GridC g;
+  if (int st = basis_grid(p, bx, bz, g, "mgb_spectral_derivative_basis")) return st;
+  if (kind < MGB_DDX || kind > MGB_NABLA2) return fail(MGB_ERR_INVALID, "unknown derivative kind %d", kind);
+  if (in == out && g.fdm && (kind != MGB_DDX && kind != MGB_D2DX2))
+    return fail(MGB_ERR_INVALID, "z stencils on FDM-z need distinct input and output");
+  k_spec_deriv<<<nblocks((size_t)g.rows * g.cols), PT, 0, s>>>(g, kind, in, out);
+  MGB_LAUNCH_CHECK();
+  return MGB_OK;
+}
+
+int pw_laplacian_basis(const mgb_plan* p, int bx, int bz, double* lap, cudaStream_t s) {
+  GridC g;
+  if (int st = basis_grid(p, bx, bz, g, "mgb_laplacian_basis")) return st;
+  k_laplacian<<<nblocks((size_t)g.rows * g.cols), PT, 0, s>>>(g, lap);
+  MGB_LAUNCH_CHECK();
+  return MGB_OK;
+}
+
+int pw_poisson_basis(const mgb_plan* p, int bx, int bz, const zd* rhs, zd* out, cudaStream_t s) {
+  GridC g;
+  if (int st = basis_grid(p, bx, bz, g, "mgb_poisson_solve_basis")) return st;
+  if (g.fdm) return fail(MGB_ERR_UNSUPPORTED, "mgb_poisson_solve_basis: fully spectral plans only");
   k_poisson_spectral<<<nblocks((size_t)g.rows * g.cols), PT, 0, s>>>(g, rhs, out);
   MGB_LAUNCH_CHECK();
   return MGB_OK;

@@ -11,6 +11,7 @@ import torch
 
 from . import _native as N
 from ._arrays import as_device, finish, native_target
+from .BasisFunctions import BasisFunctions
 
 
 class LaplacianSolver:
@@ -21,6 +22,10 @@ class LaplacianSolver:
         self._device = self._plan.device
         self._array_factory = array_factory
         self._laps = None
+        self._mirror = None
+        if basis_fns is not None and params.is_fully_spectral():
+            m = [int(b) if b in (BasisFunctions.COSINE, BasisFunctions.SINE) else 0 for b in basis_fns]
+            self._mirror = tuple(m) if any(m) else None
         if params.is_fully_spectral() and spatial_diff is not None:
             self.lap = spatial_diff.calc_lap(basis_fns)
 
@@ -50,5 +55,9 @@ class LaplacianSolver:
         dst, out = native_target(out, torch.complex128, pl.spectral_shape, self._device)
         if dst.data_ptr() == src.data_ptr() and self._params.discretisation[1] == "fdm":
             dst = torch.empty_like(src)
-        pl.call("mgb_poisson_solve", N.ptr(src), N.ptr(dst), N.stream_handle(self._device))
+        if self._mirror is None:
+            pl.call("mgb_poisson_solve", N.ptr(src), N.ptr(dst), N.stream_handle(self._device))
+        else:  # the Laplacian of the cosine / sine bases (melvin/LaplacianSolver.py:58-68)
+            pl.call("mgb_poisson_solve_basis", self._mirror[0], self._mirror[1], N.ptr(src), N.ptr(dst),
+                    N.stream_handle(self._device))
         return finish(dst, out)

@@ -91,10 +91,7 @@ class Variable:
 
     def snabla2(self):
         """sd2dx2 + sd2dz2 (melvin/Variable.py:111-113), one kernel."""
-        for ax, b in zip("xz", self._basis_functions):
-            if b not in (BasisFunctions.COMPLEX_EXP, BasisFunctions.FDM):
-                raise NotImplementedError(f"{b!r} along {ax} is not built for the GPU path")
-        return self._sd.snabla2(self.gets())
+        return self._sd.snabla2(self.gets(), tuple(self._basis_functions))
 
     def lap(self):
         return self._sd.calc_lap(self._basis_functions)

@@ -164,6 +164,11 @@ SIGNATURES = {
     "mgb_last_error": [],
     "mgb_to_physical": [_P, _P, _P, _P, _P],
     "mgb_to_spectral": [_P, _P, _P, _P, _P],
+    "mgb_to_physical_basis": [_P, _I, _I, _P, _P, _P, _P],
+    "mgb_to_spectral_basis": [_P, _I, _I, _P, _P, _P, _P],
+    "mgb_spectral_derivative_basis": [_P, _I, _I, _I, _P, _P, _P],
+    "mgb_laplacian_basis": [_P, _I, _I, _P, _P],
+    "mgb_poisson_solve_basis": [_P, _I, _I, _P, _P, _P],
     "mgb_pddx": [_P, _P, _P, _P],
     "mgb_pddz": [_P, _P, _P, _P],
     "mgb_spectral_derivative": [_P, _I, _P, _P, _P],

@@ -122,6 +122,114 @@ def to_spectral(g: Grid, p: np.ndarray) -> np.ndarray:
     return out
 
 
+# Cosine / sine bases -- melvin/SpectralTransformer.py:90-199 with
+# BasisFunctions.COSINE (1) and SINE (2) on a fully spectral grid.  A cosine
+# or sine axis of n points is the mirrored periodic signal of 2(n-1) points
+# (even extension for cosine, odd for sine); x_factor / z_factor are n, n-1
+# or -1j*(n-1); the zeroth cosine mode is doubled before the inverse and
+# halved after the forward transform.  (The reference doubles it in its
+# input array in place; this restatement works on a copy.)
+EXP, COS, SIN = 0, 1, 2
+
+
+def _axis_factor(basis, n):
+    if basis == COS:
+        return n - 1
+    if basis == SIN:
+        return -1j * (n - 1)
+    return n
+
+
+def _axis_len(basis, n):
+    return 2 * (n - 1) if basis in (COS, SIN) else n
+
+
+def to_physical_basis(g: Grid, s: np.ndarray, bx: int, bz: int) -> np.ndarray:
+    nn, nm = g.nn, g.nm
+    s = np.array(s, dtype=np.complex128, copy=True)
+    if bx == COS:
+        s[0] *= 2
+    if bz == COS:
+        s[:, 0] *= 2
+    lx = _axis_len(bx, g.nx)
+    hz = 2 * (g.nz - 1) // 2 + 1 if bz in (COS, SIN) else g.nz // 2 + 1
+    pad = np.zeros((lx, hz), dtype=np.complex128)
+    pad[: nn + 1, :nm] = s[: nn + 1, :nm]
+    pad[-nn:, :nm] = s[-nn:, :nm]
+    pad *= _axis_factor(bx, g.nx) * _axis_factor(bz, g.nz)
+    out = np.fft.irfft2(pad)
+    if bx in (COS, SIN):
+        out = out[: g.nx]
+    if bz in (COS, SIN):
+        out = out[:, : g.nz]
+    return out
+
+
+def to_spectral_basis(g: Grid, p: np.ndarray, bx: int, bz: int) -> np.ndarray:
+    nn, nm = g.nn, g.nm
+    a = np.asarray(p, dtype=np.float64)
+    if bx == COS:
+        a = np.concatenate((a[:-1], a[:0:-1]))
+    elif bx == SIN:
+        a = np.concatenate((a[:-1], -a[:0:-1]))
+    if bz == COS:
+        a = np.concatenate((a[:, :-1], a[:, :0:-1]), axis=1)
+    elif bz == SIN:
+        a = np.concatenate((a[:, :-1], -a[:, :0:-1]), axis=1)
+    f = np.fft.rfft2(a) / (_axis_factor(bx, g.nx) * _axis_factor(bz, g.nz))
+    if bx == COS:
+        f[0] /= 2
+    if bz == COS:
+        f[:, 0] /= 2
+    out = np.empty((2 * nn + 1, nm), dtype=np.complex128)
+    out[: nn + 1] = f[: nn + 1, :nm]
+    out[-nn:] = f[-nn:, :nm]
+    return out
+
+
+def _basis_dfac(basis, length):
+    # calc_diff_wavelength / L (melvin/BasisFunctions.py:26-36,44-52)
+    return {EXP: 1j * 2 * np.pi, SIN: np.pi, COS: -np.pi}[basis] / length
+
+
+def _basis_d2fac(basis, length):
+    # -|wavelength|^2 / L^2 (melvin/BasisFunctions.py:39-42,55-59)
+    return -np.abs({EXP: 1j * 2 * np.pi, SIN: np.pi, COS: -np.pi}[basis]) ** 2 / length ** 2
+
+
+def sddx_basis(g: Grid, s, bx):
+    n, _ = mode_numbers(g)
+    return _basis_dfac(bx, g.lx) * n * s
+
+
+def sddz_basis(g: Grid, s, bz):
+    _, m = mode_numbers(g)
+    return _basis_dfac(bz, g.lz) * m * s
+
+
+def sd2dx2_basis(g: Grid, s, bx):
+    n, _ = mode_numbers(g)
+    return _basis_d2fac(bx, g.lx) * n ** 2 * s
+
+
+def sd2dz2_basis(g: Grid, s, bz):
+    _, m = mode_numbers(g)
+    return _basis_d2fac(bz, g.lz) * m ** 2 * s
+
+
+def laplacian_symbol_basis(g: Grid, bx, bz):
+    n, m = mode_numbers(g)
+    return _basis_d2fac(bx, g.lx) * n ** 2 + _basis_d2fac(bz, g.lz) * m ** 2
+
+
+def poisson_basis(g: Grid, rhs, bx, bz):
+    """_solve_fully_spectral with the Laplacian of the bases, (0, 0) divided
+    by 1 (melvin/LaplacianSolver.py:58-68)."""
+    lap = laplacian_symbol_basis(g, bx, bz).astype(np.complex128)
+    lap[0, 0] = 1.0
+    return rhs / lap
+
+
 # ---------------------------------------------------------------------------
 # Finite-difference stencils -- melvin/SpatialDifferentiator.py:76-185
 # ---------------------------------------------------------------------------

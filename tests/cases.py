@@ -43,3 +43,14 @@ def params_dict(g, integrator="semi-implicit", order=2, dt=1e-3, precision="doub
         "discretisation": ["spectral", "fdm" if g.fdm_z else "spectral"], "precision": precision,
         "device": device,
     }
+
+
+# Cosine / sine basis golden cases: tag -> grid (n = 2^k + 1 on a mirrored axis),
+# basis codes in the tag suffix (0 complex exponential, 1 cosine, 2 sine).
+BASIS_TAGS = ["basis65x64_10", "basis65x64_20", "basis64x65_01", "basis64x65_02", "basis65x65_11", "basis65x65_22",
+              "basis65x65_21", "basis33x65_12"]
+
+
+def basis_grid(tag):
+    nx, nz = (int(v) for v in tag[len("basis"):].split("_")[0].split("x"))
+    return O.Grid(nx, nz, 1.0, 2.0)

@@ -109,6 +109,30 @@ def verbs(tag, p, rng):
     G[f"{tag}/am"] = sim._integrator.corrector(dv)
 
 
+def basis_verbs(tag, p, bf, rng):
+    """The reference's cosine / sine basis transforms and spectral verbs
+    (melvin/SpectralTransformer.py:90-199, melvin/SpatialDifferentiator.py:50-74,
+    melvin/LaplacianSolver.py:58-68) on seeded inputs.  to_physical doubles
+    the zeroth cosine mode of its input in place, so it gets a copy."""
+    with redirect_stdout(io.StringIO()):
+        sim = Simulation(p, np)
+    st = sim._spectral_trans
+    s = rand_spec(rng, p.spectral_shape)
+    phys = rng.standard_normal((p.nx, p.nz))
+    G[f"{tag}/in_spec"] = s
+    G[f"{tag}/in_phys"] = phys
+    G[f"{tag}/basis"] = np.array([int(bf[0]), int(bf[1])])
+    G[f"{tag}/to_physical"] = st.to_physical(s.copy(), basis_functions=bf)
+    G[f"{tag}/to_spectral"] = st.to_spectral(phys.copy(), basis_functions=bf)
+    q = sim.make_variable("q", bf)
+    q.sets(s.copy())
+    for verb in ("sddx", "sddz", "sd2dx2", "sd2dz2", "snabla2", "lap"):
+        G[f"{tag}/{verb}"] = getattr(q, verb)()
+    with redirect_stdout(io.StringIO()):
+        sim.init_laplacian_solver(bf)
+    G[f"{tag}/poisson"] = sim.get_laplacian_solver().solve(s.copy())
+
+
 def trajectory(tag, p, fields, init, nsteps, body):
     """Run `nsteps` of `body` with the reference objects; store states."""
     with redirect_stdout(io.StringIO()):
@@ -290,6 +314,14 @@ def main():
     ddc_terms = {"w": [("T", -Pr * RaT), ("S", Pr * RaT / Rr)], "T": [], "S": []}
     trajectory("ddcd32x17", p, ["w", "T", "S"], {"w": np.zeros((32, 17)), "T": t0, "S": s0}, 8,
                dirichlet_body({"w": Pr, "T": 1.0, "S": 1.0 / Le}, ddc_terms))
+
+    # ---- cosine / sine bases (n = 2^k + 1 on a mirrored axis) ----
+    rb = np.random.default_rng(2024)
+    COS, SIN = BasisFunctions.COSINE, BasisFunctions.SINE
+    for (nx, nz, bf) in [(65, 64, [COS, EXP]), (65, 64, [SIN, EXP]), (64, 65, [EXP, COS]), (64, 65, [EXP, SIN]),
+                         (65, 65, [COS, COS]), (65, 65, [SIN, SIN]), (65, 65, [SIN, COS]), (33, 65, [COS, SIN])]:
+        tag = f"basis{nx}x{nz}_{int(bf[0])}{int(bf[1])}"
+        basis_verbs(tag, params(nx, nz, 1.0, 2.0), bf, rb)
 
     np.savez_compressed(OUT, **G)
     print(f"wrote {OUT}: {len(G)} arrays, {os.path.getsize(OUT) / 1024:.1f} KiB")

@@ -171,3 +171,92 @@ def test_kh_initial_condition_sign():
     u = np.tanh((Z - np.pi) / 0.2) - np.tanh((Z - np.pi / 2) / 0.2)
     assert rel_l2(vel["ux_p"], u - u.mean()) < 1e-2
     np.testing.assert_allclose(c, -0.5 * u)
+
+
+# ---- cosine / sine bases -------------------------------------------------
+
+from cases import BASIS_TAGS, basis_grid  # noqa: E402
+
+
+@pytest.mark.parametrize("tag", BASIS_TAGS)
+def test_oracle_basis_verbs_match_reference(golden, tag):
+    from oracle import melvin_np as M
+
+    g = basis_grid(tag)
+    bx, bz = (int(v) for v in golden[f"{tag}/basis"])
+    s, p = golden[f"{tag}/in_spec"], golden[f"{tag}/in_phys"]
+    got = {
+        "to_physical": M.to_physical_basis(g, s, bx, bz),
+        "to_spectral": M.to_spectral_basis(g, p, bx, bz),
+        "sddx": M.sddx_basis(g, s, bx),
+        "sddz": M.sddz_basis(g, s, bz),
+        "sd2dx2": M.sd2dx2_basis(g, s, bx),
+        "sd2dz2": M.sd2dz2_basis(g, s, bz),
+        "snabla2": M.sd2dx2_basis(g, s, bx) + M.sd2dz2_basis(g, s, bz),
+        "lap": M.laplacian_symbol_basis(g, bx, bz),
+        "poisson": M.poisson_basis(g, s, bx, bz),
+    }
+    for k, v in got.items():
+        np.testing.assert_array_equal(v, golden[f"{tag}/{k}"], err_msg=k)
+
+
+def _kat_mgrid(nx=65, nz=65):
+    return O.Grid(nx, nz, 1.0, 1.0)
+
+
+def test_kat_transform_cosine_x_periodic_z():
+    """test/SpectralTransformer_test.py:64-97 restated at nx = 65 (2^6 + 1), nz = 64."""
+    from oracle import melvin_np as M
+
+    g = _kat_mgrid(65, 64)
+    X, Z = np.meshgrid(np.linspace(0, 1.0, g.nx), np.linspace(0, 1.0, g.nz, endpoint=False), indexing="ij")
+    phys = np.cos(np.pi * X) + 2.0 * np.cos(2 * np.pi * X)
+    spec = M.to_spectral_basis(g, phys, M.COS, M.EXP)
+    want = np.zeros(g.spectral_shape, complex)
+    want[1, 0], want[2, 0], want[-1, 0], want[-2, 0] = 1.0, 2.0, 1.0, 2.0
+    np.testing.assert_array_almost_equal(spec, want)
+    np.testing.assert_array_almost_equal(M.to_physical_basis(g, spec, M.COS, M.EXP), phys)
+
+
+def test_kat_transform_periodic_x_cosine_z():
+    """test/SpectralTransformer_test.py:100-125 restated at nx = 64, nz = 65."""
+    from oracle import melvin_np as M
+
+    g = _kat_mgrid(64, 65)
+    X, Z = np.meshgrid(np.linspace(0, 1.0, g.nx, endpoint=False), np.linspace(0, 1.0, g.nz), indexing="ij")
+    phys = np.cos(np.pi * Z) + 2.0 * np.cos(2 * np.pi * Z)
+    spec = M.to_spectral_basis(g, phys, M.EXP, M.COS)
+    want = np.zeros(g.spectral_shape, complex)
+    want[0, 1], want[0, 2] = 1.0, 2.0
+    np.testing.assert_array_almost_equal(spec, want)
+    np.testing.assert_array_almost_equal(M.to_physical_basis(g, spec, M.EXP, M.COS), phys)
+
+
+def test_kat_transform_cosine_both():
+    """test/SpectralTransformer_test.py:128-170 restated at 65 x 65."""
+    from oracle import melvin_np as M
+
+    g = _kat_mgrid()
+    X, Z = np.meshgrid(np.linspace(0, 1.0, g.nx), np.linspace(0, 1.0, g.nz), indexing="ij")
+    phys = (np.cos(np.pi * Z) + 2.0 * np.cos(2 * np.pi * Z) + np.cos(np.pi * X)
+            + 2.0 * np.cos(2 * np.pi * X) * np.cos(1 * np.pi * Z))
+    spec = M.to_spectral_basis(g, phys, M.COS, M.COS)
+    want = np.zeros(g.spectral_shape, complex)
+    want[0, 1], want[0, 2] = 1.0, 2.0
+    want[1, 0], want[2, 1], want[-1, 0], want[-2, 1] = 1.0, 2.0, 1.0, 2.0
+    np.testing.assert_array_almost_equal(spec, want)
+    np.testing.assert_array_almost_equal(M.to_physical_basis(g, spec, M.COS, M.COS), phys)
+
+
+def test_kat_transform_sine_both():
+    """test/SpectralTransformer_test.py:173-205 restated at 65 x 65."""
+    from oracle import melvin_np as M
+
+    g = _kat_mgrid()
+    X, Z = np.meshgrid(np.linspace(0, 1.0, g.nx), np.linspace(0, 1.0, g.nz), indexing="ij")
+    phys = np.sin(np.pi * Z) * np.sin(np.pi * X) + 2.0 * np.sin(2 * np.pi * Z) * np.sin(3 * np.pi * X)
+    spec = M.to_spectral_basis(g, phys, M.SIN, M.SIN)
+    want = np.zeros(g.spectral_shape, complex)
+    want[1, 1], want[-1, 1], want[3, 2], want[-3, 2] = 1.0, -1.0, 2.0, -2.0
+    np.testing.assert_array_almost_equal(spec, want)
+    np.testing.assert_array_almost_equal(M.to_physical_basis(g, spec, M.SIN, M.SIN), phys)
