@@ -625,6 +625,43 @@ def run_mixed_ensemble(args):
     return 0
 
 
+def run_ddc_pool(args):
+    """One slot pool of the solve server: 32 double-diffusive convection runs
+    on a --n x (--n + 1) Fourier-x / Dirichlet-z grid (Ra_T = 1e6, Pr = 7,
+    Le = 100, R_rho = 2, explicit AB2), advanced by batched steps."""
+    import torch
+
+    from melvin import serving
+
+    device = torch.device("cuda", dist_env()[2])
+    torch.cuda.set_device(device)
+    nx, nz, slots = args.n, args.n + 1, 32
+    srv = serving.Server(serving.DDCConfig(precision=args.precision), device=str(device))
+    pool = serving._Pool(srv, nx, nz, slots)
+    for s in range(slots):
+        pool.admit(serving.Request(rid=s, nx=nx, nz=nz, r_rho=2.0, nsteps=args.steps, seed=s), srv.cfg)
+    members = torch.arange(slots, dtype=torch.int32, device=device)
+    for _ in range(args.warmup):
+        pool.ens.step(pool.dt, members)
+    torch.cuda.synchronize()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
+    ev = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        pool.ens.step(pool.dt, members)
+        e1.record()
+        ev.append((e0, e1))
+    torch.cuda.synchronize()
+    secs = sum(a.elapsed_time(b) for a, b in ev) * 1e-3
+    print(json.dumps({"workload": "ddc-pool", "grid": f"{nx}x{nz}", "slots": slots, "precision": args.precision,
+                      "steps": args.steps, "ms_per_step": round(secs / args.steps * 1e3, 4),
+                      "value": round(slots * nx * nz * args.steps / secs / 1e6, 2), "unit": UNIT,
+                      "l2": "flushed between steps"}), flush=True)
+    return 0
+
+
 def run_serving(args):
     """Poisson stream of double-diffusive convection solves (Fourier-x /
     Dirichlet-z, grids 128x129..1024x1025, R_rho ~ U[1.5, 4], 200..2000
@@ -661,7 +698,7 @@ def main(argv=None):
     ap.add_argument("--tiles", help="pin the tile variants x-inverse,z,x-forward (e.g. 0,1,1) instead of tuning")
     ap.add_argument("--only", choices=["fp64", "split", "dfloat"],
                     help="run only the timed fused steps of one precision")
-    ap.add_argument("--workload", choices=["turbulence", "kh-ensemble", "mixed-ensemble", "serving"],
+    ap.add_argument("--workload", choices=["turbulence", "kh-ensemble", "mixed-ensemble", "ddc-pool", "serving"],
                     default="turbulence",
                     help="turbulence: the headline line; kh-ensemble / serving: the batched and serving lines")
     ap.add_argument("--members", type=int, default=256, help="kh-ensemble members")
@@ -678,6 +715,8 @@ def main(argv=None):
         return run_mixed_ensemble(args)
     if args.workload == "serving":
         return run_serving(args)
+    if args.workload == "ddc-pool":
+        return run_ddc_pool(args)
     if args.only:
         return run_only(args)
     return run_native(args)

@@ -400,7 +400,7 @@ typedef enum mgb_family {
 typedef struct mgb_tile_info {
   int32_t available;    /* 1 when the variant exists for this plan (its shared memory fits) */
   int32_t shape;        /* columns per CTA (x passes) or row pairs per CTA (z pass) */
-  int32_t radix;        /* largest FFT radix (8 or 4) */
+  int32_t radix;        /* largest FFT radix (8 or 16) */
   int32_t reserved;
   uint64_t smem_bytes;  /* dynamic shared memory per CTA */
 } mgb_tile_info;

@@ -80,7 +80,7 @@ __device__ __forceinline__ zd fd_snabla2(const GridC& g, const zd* row, int n, i
 // ---------------------------------------------------------------------------
 
 constexpr int TH_BLOCK = 8;
-constexpr int TH_THREADS = 128;
+constexpr int TH_THREADS = 32;  // one warp per CTA: the chains spread over every SM
 
 // Member = blockIdx.y; mode = blockIdx.x * TH_THREADS + threadIdx.x.
 static __global__ void __launch_bounds__(TH_THREADS) k_thomas(GridC g, Mptr rhs_p, double rhs_sign, Mptr out_p,

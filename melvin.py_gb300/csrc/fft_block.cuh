@@ -72,15 +72,66 @@ struct Dft<8, DIR, T> {
   }
 };
 
+// v * (cr + i ci) for a constant twiddle.
+template <typename T>
+__device__ __forceinline__ cx<T> ctw(cx<T> v, T cr, T ci) {
+  return mk(v.x * cr - v.y * ci, v.x * ci + v.y * cr);
+}
+
+template <int DIR, typename T>
+struct Dft<16, DIR, T> {
+  // Radix-16 as 4 x 4: with n = n1 + 4 n2 and k = 4 k1 + k2,
+  //   X[4 k1 + k2] = sum_n1 W4^(n1 k1) W16^(n1 k2) sum_n2 a[n1 + 4 n2] W4^(n2 k2),
+  // W16 = exp(DIR * 2*pi*i/16): four DFT4 over n2, the twiddles W16^(n1 k2),
+  // four DFT4 over n1.
+  static __device__ __forceinline__ void run(cx<T>* a) {
+    const T c1 = (T)0.92387953251128675612818318939678828682;  // cos(pi/8)
+    const T s1 = (T)0.38268343236508977172845998403039886676;  // sin(pi/8)
+    const T r = (T)0.70710678118654752440084436210484903928;   // cos(pi/4)
+    const T d = (T)DIR;
+    cx<T> y[4][4];
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) {
+      y[n1][0] = a[n1];
+      y[n1][1] = a[n1 + 4];
+      y[n1][2] = a[n1 + 8];
+      y[n1][3] = a[n1 + 12];
+      dft4<4, DIR>(y[n1][0], y[n1][1], y[n1][2], y[n1][3]);
+    }
+    // W16^e, e = n1 * k2: 1, 2, 3 | 2, 4, 6 | 3, 6, 9
+    y[1][1] = ctw(y[1][1], c1, d * s1);
+    y[1][2] = ctw(y[1][2], r, d * r);
+    y[1][3] = ctw(y[1][3], s1, d * c1);
+    y[2][1] = ctw(y[2][1], r, d * r);
+    y[2][2] = mul_i<DIR>(y[2][2]);
+    y[2][3] = ctw(y[2][3], -r, d * r);
+    y[3][1] = ctw(y[3][1], s1, d * c1);
+    y[3][2] = ctw(y[3][2], -r, d * r);
+    y[3][3] = ctw(y[3][3], -c1, -(d * s1));
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) {
+      cx<T> z0 = y[0][k2], z1 = y[1][k2], z2 = y[2][k2], z3 = y[3][k2];
+      dft4<4, DIR>(z0, z1, z2, z3);
+      a[k2] = z0;
+      a[4 + k2] = z1;
+      a[8 + k2] = z2;
+      a[12 + k2] = z3;
+    }
+  }
+};
+
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
 // Radix of the pass that starts with sub-transform length NS, at most RM
-// (8 or 4).  With RM = 8 a remaining length of 16 is split 4 x 4 rather than
-// 8 x 2, so no radix-2 pass follows a radix-8 one.
+// (16 or 8).  The tail avoids a radix-2 pass: with RM = 8 a remaining length
+// of 16 is split 4 x 4 rather than 8 x 2, with RM = 16 a remaining 32 is
+// split 8 x 4 rather than 16 x 2.
 template <int N, int NS, int RM>
 struct PassRadix {
   static constexpr int rem = N / NS;
-  static constexpr int value = (RM >= 8 && rem >= 8 && rem != 16) ? 8 : (rem >= 4 ? 4 : 2);
+  static constexpr int value = (RM >= 16 && rem >= 16 && rem != 32)
+                                   ? 16
+                                   : ((rem >= 8 && rem != 16) ? 8 : (rem >= 4 ? 4 : 2));
 };
 
 template <typename T, int N, int C, int CS, int NT, int DIR, int R, int NS>
@@ -142,7 +193,7 @@ struct FftPasses<T, N, C, CS, NT, DIR, RM, NS, true> {
 template <typename T, int N, int C, int CS, int NT, int DIR, int RM = 8>
 __device__ __forceinline__ void block_fft(cx<T>* buf, const cx<T>* __restrict__ tw) {
   static_assert((N & (N - 1)) == 0 && N >= 4, "power-of-two length");
-  static_assert(RM == 8 || RM == 4, "maximum radix 8 or 4");
+  static_assert(RM == 16 || RM == 8, "maximum radix 16 or 8");
   FftPasses<T, N, C, CS, NT, DIR, RM, 1>::run(buf, tw);
 }
 

@@ -71,9 +71,9 @@ struct XTile {
 // of advected fields) by an autotuner that times them on the caller's own
 // workload.  Variant 0 is the default.
 //   x passes (k_xinv, k_xf_step): columns per CTA C and maximum FFT radix
-//     v = 0: C = XTile::C, radix 8; v = 1: C/2; v = 2: 2C; v = 3: C, radix 4
+//     v = 0: C = XTile::C, radix 8; v = 1: C/2; v = 2: 2C; v = 3: C, radix 16
 //   z pass (k_zz_step): row pairs per CTA P and maximum FFT radix
-//     v = 0: P = 1, radix 8; v = 1: P = 2; v = 2: P = 4; v = 3: P = 1, radix 4
+//     v = 0: P = 1, radix 8; v = 1: P = 2; v = 2: P = 4; v = 3: P = 1, radix 16
 // Variants with the same shape share one kernel; those whose shared memory
 // does not fit are absent.  Columns and row pairs change only which CTA does
 // the work, so they give bit-identical results; the radix changes rounding.
@@ -84,13 +84,13 @@ struct XVar {
   static constexpr int C0 = XTile<T, N>::C;
   static constexpr int Cr = V == 1 ? C0 / 2 : (V == 2 ? 2 * C0 : C0);
   static constexpr int C = Cr < 1 ? 1 : (Cr > 64 ? 64 : Cr);
-  static constexpr int RM = V == 3 ? 4 : 8;
+  static constexpr int RM = V == 3 ? 16 : 8;
 };
 
 template <int V>
 struct ZVar {
   static constexpr int P = V == 1 ? 2 : (V == 2 ? 4 : 1);
-  static constexpr int RM = V == 3 ? 4 : 8;
+  static constexpr int RM = V == 3 ? 16 : 8;
 };
 
 // Largest dynamic shared memory a CTA may request (227 KB minus the static

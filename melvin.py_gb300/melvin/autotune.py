@@ -17,7 +17,7 @@ the end, so tuning can happen at any point of a run.  A CUDA graph captured
 before tuning keeps the kernels it captured; capture after tuning.
 
 Variants that differ only in columns or row pairs per CTA give bit-identical
-results; a radix-4 variant changes the rounding of the transforms (the FP64
+results; the radix-16 variant changes the rounding of the transforms (the FP64
 path stays within the 1e-12 parity bound of every variant).
 
 The reference has no counterpart: numpy.fft picks its own factorisation

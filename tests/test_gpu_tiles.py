@@ -5,7 +5,7 @@
   reference trajectories (golden vectors), and against the oracle on larger
   grids.
 * Variants that differ only in columns or row pairs per CTA give
-  bit-identical states; a radix-4 variant stays within 1e-13 (FP64) or
+  bit-identical states; the radix-16 variant stays within 1e-13 (FP64) or
   1e-6 (split precision) of the default.
 * The tuner leaves the stepped object's state bit-identical to what it
   was, and the selection it sets steps like the default.
