@@ -2,7 +2,7 @@
 loop against the reference trajectories (golden vectors) and the oracle.
 
 Tolerances: FP64 paths 1e-12 relative L2 of every field after every step
-(the spec per-step bound); the split-precision path (FP32
+(the parity bound of the FP64 path); the split-precision path (FP32
 transforms, FP64 state) is checked against the FP64 oracle at 1e-5 after
 the trajectory."""
 
