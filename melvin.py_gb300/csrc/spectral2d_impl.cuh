@@ -33,18 +33,22 @@ namespace mgb {
 
 // Resident CTAs per SM the compiler must allow for (register budget).  The
 // FP32 and double-float kernels are latency bound (global loads, chains of
-// dependent FP32 ops), so they ask for three and two 256-thread CTAs per SM;
-// the FP64 kernels are bound by the FP64 pipe and keep the default.
-template <typename T>
+// dependent FP32 ops), so they ask for several 256-thread CTAs per SM: four
+// (64 registers) for FP32 transforms of up to 512 points, three (80
+// registers) for longer ones, whose larger butterfly sets spill at 64
+// (measured: the 256-point KH ensemble step is 6% faster with four, the
+// 2048-point turbulence step 4% slower); two for double-float.  The FP64
+// kernels are bound by the FP64 pipe and keep the default.
+template <typename T, int N>
 struct MinCTAs {
   static constexpr int value = 1;
 };
-template <>
-struct MinCTAs<float> {
-  static constexpr int value = 3;
+template <int N>
+struct MinCTAs<float, N> {
+  static constexpr int value = N <= 512 ? 4 : 3;
 };
-template <>
-struct MinCTAs<df64> {
+template <int N>
+struct MinCTAs<df64, N> {
   static constexpr int value = 2;
 };
 
@@ -52,10 +56,11 @@ struct MinCTAs<df64> {
 // but no more than its shared memory lets reside (228 KB per SM, 1 KB of it
 // reserved per CTA), so a large tile is not squeezed into registers for
 // CTAs that could never be resident together.
-template <typename T, size_t SMEM>
+template <typename T, int N, size_t SMEM>
 struct Occ {
   static constexpr int by_smem = (int)(233472 / (SMEM + 1024));
-  static constexpr int value = by_smem < 1 ? 1 : (by_smem < MinCTAs<T>::value ? by_smem : MinCTAs<T>::value);
+  static constexpr int value =
+      by_smem < 1 ? 1 : (by_smem < MinCTAs<T, N>::value ? by_smem : MinCTAs<T, N>::value);
 };
 
 // Columns per CTA of an x pass: 4096 complex values in shared memory
@@ -156,7 +161,7 @@ struct XinvArgs {
 constexpr int kXLoads = 4;
 
 template <typename T, int N, int C, int RM>
-__global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<T, C>(N) * sizeof(cx<T>)>::value)) k_xinv(const XinvArgs a) {
+__global__ void __launch_bounds__(NT, (Occ<T, N, sbuf_elems<T, C>(N) * sizeof(cx<T>)>::value)) k_xinv(const XinvArgs a) {
   if (gate_closed(a.b.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
@@ -361,7 +366,7 @@ struct ZzLayout {
 };
 
 template <typename T, int N, int F, int P, int RM>
-__global__ void __launch_bounds__(NT, (Occ<T, sbuf_elems<T, ZzLayout<T, F, P>::value>(N) * sizeof(cx<T>)>::value))
+__global__ void __launch_bounds__(NT, (Occ<T, N, sbuf_elems<T, ZzLayout<T, F, P>::value>(N) * sizeof(cx<T>)>::value))
     k_zz_step(const ZzArgs a) {
   if (gate_closed(a.b.gate)) return;
   constexpr int NIN = ZzShape<F, P>::NIN, NOUT = ZzShape<F, P>::NOUT, CS = ZzLayout<T, F, P>::value;
@@ -529,7 +534,7 @@ struct XfLoads {
 };
 
 template <typename T, int N, int F, int C, int RM>
-__global__ void __launch_bounds__(NT, (Occ<T, F * sbuf_elems<T, C>(N) * sizeof(cx<T>)>::value))
+__global__ void __launch_bounds__(NT, (Occ<T, N, F * sbuf_elems<T, C>(N) * sizeof(cx<T>)>::value))
     k_xf_step(const XfArgs a) {
   if (gate_closed(a.b.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
