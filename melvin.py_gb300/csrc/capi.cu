@@ -106,6 +106,8 @@ static void release(mgb_plan* p) {
   cudaFree(p->tab_df);
   cudaFree(p->th_inv);
   cudaFree(p->th_cp);
+  cudaFree(p->th_ps);
+  cudaFree(p->th_qs);
   cudaFree(p->tab_d);
   cudaFree(p->tab_f);
   delete p;

@@ -1,5 +1,7 @@
 // Host orchestration of the Fourier-x / Dirichlet-z kernels, plus the two
 // small physical stencil kernels of the per-verb API.
+#include <algorithm>
+#include <utility>
 #include <vector>
 
 #include "fdm_impl.cuh"
@@ -90,11 +92,25 @@ inline int grid_for(size_t n) {
   return (int)(b > 152 * 16 ? 152 * 16 : (b < 1 ? 1 : b));
 }
 
+template <int G>
+void launch_thomas(const mgb_plan* p, Mptr rhs, double sign, Mptr out, const int* members, int nb, cudaStream_t s,
+                   Gate gate) {
+  const GridC& g = p->g;
+  const int blocks = (g.nn * G + TH_THREADS - 1) / TH_THREADS;
+  k_thomas<G><<<dim3(blocks, nb), TH_THREADS, 0, s>>>(g, rhs, sign, out, members, p->th_inv, p->th_cp, p->th_ps,
+                                                     p->th_qs, gate);
+}
+
 int thomas(const mgb_plan* p, Mptr rhs, double sign, Mptr out, const int* members, int nb, cudaStream_t s,
            Gate gate) {
-  const GridC& g = p->g;
-  k_thomas<<<dim3((g.nn + TH_THREADS - 1) / TH_THREADS, nb), TH_THREADS, 0, s>>>(g, rhs, sign, out, members,
-                                                                              p->th_inv, p->th_cp, gate);
+  switch (thomas_lanes(p->g.nz)) {
+    case 1: launch_thomas<1>(p, rhs, sign, out, members, nb, s, gate); break;
+    case 2: launch_thomas<2>(p, rhs, sign, out, members, nb, s, gate); break;
+    case 4: launch_thomas<4>(p, rhs, sign, out, members, nb, s, gate); break;
+    case 8: launch_thomas<8>(p, rhs, sign, out, members, nb, s, gate); break;
+    case 16: launch_thomas<16>(p, rhs, sign, out, members, nb, s, gate); break;
+    default: launch_thomas<32>(p, rhs, sign, out, members, nb, s, gate); break;
+  }
   MGB_LAUNCH_CHECK();
   return MGB_OK;
 }
@@ -104,7 +120,7 @@ int thomas(const mgb_plan* p, Mptr rhs, double sign, Mptr out, const int* member
 int fd_plan_init(mgb_plan* p) {
   const GridC& g = p->g;
   const size_t n = (size_t)g.nn * g.nz;
-  std::vector<double> ip(n, 0.0), cp(n, 0.0);
+  std::vector<double> ip(n, 0.0), cp(n, 0.0), ps(n, 0.0), qs(n, 0.0);
   const double a = 1.0 / (g.dz * g.dz);
   const double kx = g.dfx;  // |2*pi*i/lx|
   for (int m = 0; m < g.nn; ++m) {
@@ -123,11 +139,24 @@ int fd_plan_init(mgb_plan* p) {
     }
     ipm[g.nz - 1] = 1.0;
     cpm[g.nz - 1] = 0.0;
+    // the segment products of the segmented sweeps: P_j = prod_{i=s..j}
+    // (-a ip_i) forward, Q_j = prod_{i=j..e-1} (-cp_i) backward, per segment
+    // [s, e) of TH_SEG interior rows
+    double* psm = ps.data() + (size_t)m * g.nz;
+    double* qsm = qs.data() + (size_t)m * g.nz;
+    for (int s0 = 1; s0 < g.nz - 1; s0 += TH_SEG) {
+      const int s1 = std::min(s0 + TH_SEG, g.nz - 1);
+      double pr = 1.0, qr = 1.0;
+      for (int j = s0; j < s1; ++j) psm[j] = pr *= -a * ipm[j];
+      for (int j = s1 - 1; j >= s0; --j) qsm[j] = qr *= -cpm[j];
+    }
   }
-  MGB_CUDA(cudaMalloc(&p->th_inv, n * sizeof(double)));
-  MGB_CUDA(cudaMalloc(&p->th_cp, n * sizeof(double)));
-  MGB_CUDA(cudaMemcpy(p->th_inv, ip.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-  MGB_CUDA(cudaMemcpy(p->th_cp, cp.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  const std::pair<double**, const std::vector<double>*> arrays[] = {
+      {&p->th_inv, &ip}, {&p->th_cp, &cp}, {&p->th_ps, &ps}, {&p->th_qs, &qs}};
+  for (const auto& [dst, src] : arrays) {
+    MGB_CUDA(cudaMalloc(dst, n * sizeof(double)));
+    MGB_CUDA(cudaMemcpy(*dst, src->data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  }
   return MGB_OK;
 }
 

@@ -68,83 +68,187 @@ __device__ __forceinline__ zd fd_snabla2(const GridC& g, const zd* row, int n, i
 }
 
 // ---------------------------------------------------------------------------
-// Thomas solve of the per-mode Dirichlet Poisson systems.  The factors
-// (inverse pivots and modified upper diagonal) are precomputed per plan.
-// One thread solves one mode of one member, its real and imaginary parts as
-// two interleaved dependency chains.  A thread streams its own row in blocks
-// of TH_BLOCK points: the loads of a block are issued before the block's
-// dependent arithmetic, so the chain waits on the FP64 latency only, and a
-// block is a whole 128-byte line of the row.  The forward sweep leaves its
-// result in `out`, which the backward sweep reads back.  `out` may alias
-// the right-hand side: every element is read before it is written.
+// Thomas solve of the per-mode Dirichlet Poisson systems, segmented.
+//
+// The factors (inverse pivots ip, modified upper diagonal cp) are
+// precomputed per plan.  The forward sweep y_j = (r_j - a y_{j-1}) ip_j and
+// the back substitution x_j = y_j - cp_j x_{j+1} are first-order linear
+// recurrences, so a sweep over a segment started from zero differs from the
+// true one by the carried value times a product of coefficients:
+//   y_j = yh_j + P_j y_{s-1},  P_j = prod_{i=s..j} (-a ip_i)
+//   x_j = xh_j + Q_j x_{e},    Q_j = prod_{i=j..e-1} (-cp_i)
+// for a segment [s, e).  The interior rows 1..nz-2 are cut into segments of
+// TH_SEG rows (fixed per grid; P and Q are precomputed per plan).  G lanes of
+// a warp solve one mode: a round covers G consecutive segments, one per lane;
+// each lane sweeps its segment from zero in registers, the segment maps
+// c -> P c + yh are composed across the G lanes by a shuffle scan, and each
+// lane adds its correction.  The lane that starts where the previous round
+// ended sweeps from the known carry and needs no correction, so with G = 1
+// this is the plain sequential sweep.  G depends on nz only, so a mode gives
+// the same bits whatever the batch around it.  `out` may alias the
+// right-hand side: a lane reads its rows before writing them, and rows 0 and
+// nz-1 are read by every lane before the first write.
 // ---------------------------------------------------------------------------
 
-constexpr int TH_BLOCK = 8;
-constexpr int TH_THREADS = 32;  // one warp per CTA: the chains spread over every SM
+constexpr int TH_SEG = 16;
+constexpr int TH_THREADS = 32;  // one warp per CTA: the modes spread over every SM
 
-// Member = blockIdx.y; mode = blockIdx.x * TH_THREADS + threadIdx.x.
-static __global__ void __launch_bounds__(TH_THREADS) k_thomas(GridC g, Mptr rhs_p, double rhs_sign, Mptr out_p,
-                                                      const int* members, const double* __restrict__ inv_piv,
-                                                      const double* __restrict__ cp, Gate gate) {
+// Lanes per mode: one segment per lane per round, at most a warp.
+inline int thomas_lanes(int nz) {
+  const int segs = (nz - 2 + TH_SEG - 1) / TH_SEG;
+  int G = 1;
+  while (G < 32 && G < segs) G *= 2;
+  return G;
+}
+
+// Member = blockIdx.y; mode = (blockIdx.x * TH_THREADS + threadIdx.x) / G.
+template <int G>
+static __global__ void __launch_bounds__(TH_THREADS)
+    k_thomas(GridC g, Mptr rhs_p, double rhs_sign, Mptr out_p, const int* members, const double* __restrict__ inv_piv,
+             const double* __restrict__ cp, const double* __restrict__ pseg, const double* __restrict__ qseg,
+             Gate gate) {
   if (gate_closed(gate)) return;
-  const int n = blockIdx.x * TH_THREADS + threadIdx.x;
-  if (n >= g.nn) return;
+  const int lane = threadIdx.x & 31;
+  const int gl = lane & (G - 1);
+  const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+  const int n = (blockIdx.x * TH_THREADS + threadIdx.x) / G;
+  if (n >= g.nn) return;  // whole groups leave together
   const int nz = g.nz;
-  const zd* rhs = (const zd*)maddr(rhs_p, members, blockIdx.y) + (size_t)n * nz;
-  zd* out = (zd*)maddr(out_p, members, blockIdx.y) + (size_t)n * nz;
-  const double* ip = inv_piv + (size_t)n * nz;
-  const double* c = cp + (size_t)n * nz;
+  const size_t fo = (size_t)n * nz;
+  const zd* rhs = (const zd*)maddr(rhs_p, members, blockIdx.y) + fo;
+  zd* out = (zd*)maddr(out_p, members, blockIdx.y) + fo;
+  const double* ip = inv_piv + fo;
+  const double* c = cp + fo;
+  const double* ps = pseg + fo;
+  const double* qs = qseg + fo;
   const double a = 1.0 / (g.dz * g.dz);
   // rhs_sign is +1 or -1, applied as a negation (exact, and no multiply the
   // compiler could fuse into the sweep's FMA)
   const bool neg = rhs_sign < 0;
-  // forward sweep: rows 0 and nz-1 are identity rows
-  zd prev = rhs[0];
-  if (neg) prev = mk(-prev.x, -prev.y);
-  out[0] = prev;
-  for (int j0 = 1; j0 < nz - 1; j0 += TH_BLOCK) {
-    zd r[TH_BLOCK];
-    double q[TH_BLOCK];
-#pragma unroll
-    for (int u = 0; u < TH_BLOCK; ++u) {
-      const int j = j0 + u;
-      r[u] = j < nz - 1 ? rhs[j] : mk(0.0, 0.0);
-      q[u] = j < nz - 1 ? ip[j] : 0.0;
-    }
-#pragma unroll
-    for (int u = 0; u < TH_BLOCK; ++u)
-      if (neg) r[u] = mk(-r[u].x, -r[u].y);
-#pragma unroll
-    for (int u = 0; u < TH_BLOCK; ++u) {
-      const int j = j0 + u;
-      if (j >= nz - 1) break;
-      const zd v = mk((r[u].x - a * prev.x) * q[u], (r[u].y - a * prev.y) * q[u]);
-      out[j] = v;
-      prev = v;
-    }
+  zd y0 = rhs[0], yl = rhs[nz - 1];  // identity end rows
+  if (neg) {
+    y0 = -y0;
+    yl = -yl;
   }
-  zd last = rhs[nz - 1];
-  if (neg) last = mk(-last.x, -last.y);
-  out[nz - 1] = last;
+  __syncwarp(gmask);
+  constexpr int R = G * TH_SEG;
+  const int rounds = (nz - 2 + R - 1) / R;
+
+  // forward sweep
+  zd carry = y0;
+  for (int rd = 0; rd < rounds; ++rd) {
+    const int js = 1 + rd * R + gl * TH_SEG;
+    const int cnt = min(max(nz - 1 - js, 0), TH_SEG);
+    zd v[TH_SEG];
+    double q[TH_SEG];
+#pragma unroll
+    for (int u = 0; u < TH_SEG; ++u) {
+      v[u] = u < cnt ? rhs[js + u] : mk(0.0, 0.0);
+      q[u] = u < cnt ? ip[js + u] : 0.0;
+    }
+    if (neg) {
+#pragma unroll
+      for (int u = 0; u < TH_SEG; ++u) v[u] = -v[u];
+    }
+    const bool first = gl == 0;
+    zd prev = first ? carry : mk(0.0, 0.0);
+#pragma unroll
+    for (int u = 0; u < TH_SEG; ++u) {
+      if (u < cnt) {
+        prev = mk((v[u].x - a * prev.x) * q[u], (v[u].y - a * prev.y) * q[u]);
+        v[u] = prev;
+      }
+    }
+    if constexpr (G > 1) {
+      double A = first ? 0.0 : (cnt > 0 ? ps[js + cnt - 1] : 1.0);
+      zd B = prev;
+#pragma unroll
+      for (int d = 1; d < G; d <<= 1) {
+        const double Ao = __shfl_up_sync(gmask, A, d, G);
+        const double Bx = __shfl_up_sync(gmask, B.x, d, G);
+        const double By = __shfl_up_sync(gmask, B.y, d, G);
+        if (gl >= d) {
+          B = mk(fma(A, Bx, B.x), fma(A, By, B.y));
+          A *= Ao;
+        }
+      }
+      // B is now y at the end of this lane's segment (lane 0's map is constant)
+      const double cx = __shfl_up_sync(gmask, B.x, 1, G);
+      const double cy = __shfl_up_sync(gmask, B.y, 1, G);
+      carry = mk(__shfl_sync(gmask, B.x, G - 1, G), __shfl_sync(gmask, B.y, G - 1, G));
+      if (!first) {
+#pragma unroll
+        for (int u = 0; u < TH_SEG; ++u)
+          if (u < cnt) {
+            const double p = ps[js + u];
+            v[u] = mk(fma(p, cx, v[u].x), fma(p, cy, v[u].y));
+          }
+      }
+    } else {
+      carry = prev;
+    }
+#pragma unroll
+    for (int u = 0; u < TH_SEG; ++u)
+      if (u < cnt) out[js + u] = v[u];
+  }
+
   // back substitution
-  zd next = last;
-  for (int j0 = nz - 2; j0 >= 1; j0 -= TH_BLOCK) {
-    zd y[TH_BLOCK];
-    double cc[TH_BLOCK];
+  carry = yl;
+  for (int rd = rounds - 1; rd >= 0; --rd) {
+    const int js = 1 + rd * R + gl * TH_SEG;
+    const int cnt = min(max(nz - 1 - js, 0), TH_SEG);
+    const int jend = min(1 + (rd + 1) * R, nz - 1);
+    zd v[TH_SEG];
+    double cc[TH_SEG];
 #pragma unroll
-    for (int u = 0; u < TH_BLOCK; ++u) {
-      const int j = j0 - u;
-      y[u] = j >= 1 ? out[j] : mk(0.0, 0.0);
-      cc[u] = j >= 1 ? c[j] : 0.0;
+    for (int u = 0; u < TH_SEG; ++u) {
+      v[u] = u < cnt ? out[js + u] : mk(0.0, 0.0);
+      cc[u] = u < cnt ? c[js + u] : 0.0;
+    }
+    const bool first = cnt > 0 && js + cnt == jend;  // the lane the carry enters
+    zd next = first ? carry : mk(0.0, 0.0);
+#pragma unroll
+    for (int u = TH_SEG - 1; u >= 0; --u) {
+      if (u < cnt) {
+        next = mk(v[u].x - cc[u] * next.x, v[u].y - cc[u] * next.y);
+        v[u] = next;
+      }
+    }
+    if constexpr (G > 1) {
+      double A = first ? 0.0 : (cnt > 0 ? qs[js] : 1.0);
+      zd B = next;
+#pragma unroll
+      for (int d = 1; d < G; d <<= 1) {
+        const double Ao = __shfl_down_sync(gmask, A, d, G);
+        const double Bx = __shfl_down_sync(gmask, B.x, d, G);
+        const double By = __shfl_down_sync(gmask, B.y, d, G);
+        if (gl + d < G) {
+          B = mk(fma(A, Bx, B.x), fma(A, By, B.y));
+          A *= Ao;
+        }
+      }
+      // B is now x at the start of this lane's segment
+      const double cx = __shfl_down_sync(gmask, B.x, 1, G);
+      const double cy = __shfl_down_sync(gmask, B.y, 1, G);
+      carry = mk(__shfl_sync(gmask, B.x, 0, G), __shfl_sync(gmask, B.y, 0, G));
+      if (!first) {
+#pragma unroll
+        for (int u = 0; u < TH_SEG; ++u)
+          if (u < cnt) {
+            const double q = qs[js + u];
+            v[u] = mk(fma(q, cx, v[u].x), fma(q, cy, v[u].y));
+          }
+      }
+    } else {
+      carry = next;
     }
 #pragma unroll
-    for (int u = 0; u < TH_BLOCK; ++u) {
-      const int j = j0 - u;
-      if (j < 1) break;
-      const zd v = mk(y[u].x - cc[u] * next.x, y[u].y - cc[u] * next.y);
-      out[j] = v;
-      next = v;
-    }
+    for (int u = 0; u < TH_SEG; ++u)
+      if (u < cnt) out[js + u] = v[u];
+  }
+  if (gl == 0) {
+    out[0] = y0;
+    out[nz - 1] = yl;
   }
 }
 

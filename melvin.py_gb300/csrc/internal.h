@@ -35,6 +35,8 @@ struct mgb_plan {
   // [nn][nz] each (inverse pivots and modified upper diagonals).
   double* th_inv = nullptr;
   double* th_cp = nullptr;
+  double* th_ps = nullptr;  // segment products of the segmented Thomas sweeps
+  double* th_qs = nullptr;
   // Fully spectral: per-mode inversion factors tux, tuz, rlap (double,
   // 3 x rows*cols) and tux, tuz (float, 2 x rows*cols).
   double* tab_d = nullptr;
