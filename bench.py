@@ -662,6 +662,51 @@ def run_ddc_pool(args):
     return 0
 
 
+def run_rbc(args):
+    """Rayleigh-Benard convection, one simulation: 1024 x 513 Fourier-x /
+    Dirichlet-z grid, lx = 2, lz = 1, Ra = 1e7, Pr = 1, 4th-order finite
+    differences in z, AB4/AM4 predictor-corrector, dt = 1e-6 (the reference's
+    examples/rayleigh_benard_convection.py); temperature the conductive
+    profile plus 1e-3 seeded noise, vorticity zero.  FP64 unless --precision
+    says otherwise."""
+    import torch
+
+    import melvin
+    from melvin import BasisFunctions as B, equations, workloads
+
+    device = torch.device("cuda", dist_env()[2])
+    torch.cuda.set_device(device)
+    nx, nz, prec = 1024, 513, args.precision
+    p = melvin.Parameters({"nx": nx, "nz": nz, "lx": 2.0, "lz": 1.0, "final_time": 1.0, "initial_dt": 1e-6,
+                           "discretisation": ["spectral", "fdm"], "integrator": "explicit", "integrator_order": 4,
+                           "spatial_derivative_order": 4, "precision": prec, "device": str(device)})
+    sim = melvin.Simulation(p, torch)
+    bf = [B.COMPLEX_EXP, B.FDM]
+    w, dw = sim.make_variable("w", bf), sim.make_derivative("dw")
+    t, dt_ = sim.make_variable("tmp", bf), sim.make_derivative("dtmp")
+    t.load(workloads.conductive(nx, nz, 2.0, 1.0, seed=0), is_physical=True)
+    step = equations.rayleigh_benard(sim, w, dw, t, dt_, 1.0, 1e7, integrator="pece")
+    for _ in range(args.warmup):
+        step.step()
+    torch.cuda.synchronize()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
+    ev = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        step.step()
+        e1.record()
+        ev.append((e0, e1))
+    torch.cuda.synchronize()
+    secs = sum(a.elapsed_time(b) for a, b in ev) * 1e-3
+    print(json.dumps({"workload": "rbc", "grid": f"{nx}x{nz}", "integrator": "AB4/AM4 predictor-corrector",
+                      "precision": prec, "steps": args.steps, "ms_per_step": round(secs / args.steps * 1e3, 4),
+                      "value": round(nx * nz * args.steps / secs / 1e6, 2), "unit": UNIT,
+                      "l2": "flushed between steps"}), flush=True)
+    return 0
+
+
 def run_serving(args):
     """Poisson stream of double-diffusive convection solves (Fourier-x /
     Dirichlet-z, grids 128x129..1024x1025, R_rho ~ U[1.5, 4], 200..2000
@@ -698,13 +743,17 @@ def main(argv=None):
     ap.add_argument("--tiles", help="pin the tile variants x-inverse,z,x-forward (e.g. 0,1,1) instead of tuning")
     ap.add_argument("--only", choices=["fp64", "split", "dfloat"],
                     help="run only the timed fused steps of one precision")
-    ap.add_argument("--workload", choices=["turbulence", "kh-ensemble", "mixed-ensemble", "ddc-pool", "serving"],
+    ap.add_argument("--workload", choices=["turbulence", "kh-ensemble", "mixed-ensemble", "ddc-pool", "serving", "rbc"],
                     default="turbulence",
-                    help="turbulence: the headline line; kh-ensemble / serving: the batched and serving lines")
+                    help="turbulence: the headline line; kh-ensemble / serving: the batched and serving lines; "
+                         "rbc: one Rayleigh-Benard simulation on a Dirichlet grid")
     ap.add_argument("--members", type=int, default=256, help="kh-ensemble members")
     ap.add_argument("--requests", type=int, default=200, help="serving requests")
-    ap.add_argument("--precision", default="split", help="precision of the kh-ensemble / serving workloads")
+    ap.add_argument("--precision", help="precision of the kh-ensemble / serving workloads (default split) "
+                                        "and of rbc (default double)")
     args = ap.parse_args(argv)
+    if args.precision is None:
+        args.precision = "double" if args.workload == "rbc" else "split"
     if args.warmup < 3 and args.impl == "native":
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
@@ -717,6 +766,8 @@ def main(argv=None):
         return run_serving(args)
     if args.workload == "ddc-pool":
         return run_ddc_pool(args)
+    if args.workload == "rbc":
+        return run_rbc(args)
     if args.only:
         return run_only(args)
     return run_native(args)
