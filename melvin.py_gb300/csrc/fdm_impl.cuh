@@ -325,10 +325,10 @@ struct FdXinvArgs {
   Gate gate;
 };
 
-template <typename T, int N>
+template <typename T, int N, int CP>
 __global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
   if (gate_closed(a.gate)) return;
-  constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
+  constexpr int C = 2 * CP;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const GridC& g = a.g;
@@ -603,11 +603,11 @@ __device__ __forceinline__ zd fd_bc(zd v, int bc, int n, int z, int nz, int e) {
   return v;
 }
 
-template <typename T, int N, int F>
+template <typename T, int N, int F, int CP>
 __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
   if (gate_closed(a.gate)) return;
   const double dt = a.gate.dt ? *a.gate.dt : a.dt;
-  constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
+  constexpr int C = 2 * CP;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const GridC& g = a.g;
@@ -705,29 +705,86 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
 // Launchers
 // ---------------------------------------------------------------------------
 
+// Column pairs per CTA of an FDM x pass: FdTile's count, or a half or a
+// quarter of it.  The arithmetic of a column does not depend on the tile, so
+// the choice is free per launch (measured on GB300 over single simulations
+// and 32-slot pools, 128x129 .. 1024x1025):
+//  * the x-inverse pass takes tiles of at most 1024 elements in FP64 (its FFT
+//    is bound by the FP64 pipe and gains from more resident warps), and in
+//    FP32 tiles of 2048 elements below length 512, FdTile's from 512 on;
+//  * the x-forward pass takes the widest tile that still gives 1.5 CTAs per
+//    SM (a single simulation on a short z axis narrows it; pools keep it).
+// Double-float keeps FdTile's count (compile time).
+inline int fd_sm_count() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    return cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0 ? v : 152;
+  }();
+  return n;
+}
+
 template <typename T, int N>
-cudaError_t launch_fd_xinv(const FdXinvArgs& a, int njobs, int nb, cudaStream_t s) {
-  constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
+struct FdCps {
+  static constexpr int c0 = FdTile<T, N>::CP;
+  static constexpr bool narrow = !std::is_same<T, df64>::value;
+  static constexpr int c1 = narrow && c0 > 1 ? c0 / 2 : c0;
+  static constexpr int c2 = narrow && c1 > 1 ? c1 / 2 : c1;
+  static constexpr int kInvElems = std::is_same<T, double>::value ? 1024 : (N >= 512 ? 4096 : 2048);
+  static int xinv() {
+    for (int cp : {c0, c1}) if (cp * N <= kInvElems) return cp;
+    return c2;
+  }
+  static int xfwd(int nz, int nb) {
+    for (int cp : {c0, c1}) {
+      const long long ctas = (long long)((nz + 2 * cp - 1) / (2 * cp)) * nb;
+      if (2 * ctas >= 3LL * fd_sm_count()) return cp;
+    }
+    return c2;
+  }
+};
+
+template <typename T, int N, int CP>
+cudaError_t launch_fd_xinv_cp(const FdXinvArgs& a, int njobs, int nb, cudaStream_t s) {
+  constexpr int C = 2 * CP;
   const size_t smem = (size_t)sbuf_elems<T, CP>(N) * sizeof(cx<T>);
-  cudaError_t e = prep_smem(k_fd_xinv<T, N>, smem);
+  cudaError_t e = prep_smem(k_fd_xinv<T, N, CP>, smem);
   if (e != cudaSuccess) return e;
   dim3 grid((a.g.nz + C - 1) / C, njobs, nb);
-  k_fd_xinv<T, N><<<grid, NT, smem, s>>>(a);
+  k_fd_xinv<T, N, CP><<<grid, NT, smem, s>>>(a);
   return cudaGetLastError();
 }
 
-template <typename T, int N, int F>
-cudaError_t launch_fd_xfwd(const FdXfArgs& a, int nb, cudaStream_t s) {
-  constexpr int CP = FdTile<T, N>::CP, C = FdTile<T, N>::C;
+template <typename T, int N>
+cudaError_t launch_fd_xinv(const FdXinvArgs& a, int njobs, int nb, cudaStream_t s) {
+  using K = FdCps<T, N>;
+  const int cp = K::xinv();
+  if (cp == K::c2) return launch_fd_xinv_cp<T, N, K::c2>(a, njobs, nb, s);
+  if (cp == K::c1) return launch_fd_xinv_cp<T, N, K::c1>(a, njobs, nb, s);
+  return launch_fd_xinv_cp<T, N, K::c0>(a, njobs, nb, s);
+}
+
+template <typename T, int N, int F, int CP>
+cudaError_t launch_fd_xfwd_cp(const FdXfArgs& a, int nb, cudaStream_t s) {
+  constexpr int C = 2 * CP;
   constexpr size_t smem = (size_t)F * sbuf_elems<T, CP>(N) * sizeof(cx<T>);
   if constexpr (smem > kMaxDynSmem) {
     return cudaErrorInvalidConfiguration;
   } else {
-    cudaError_t e = prep_smem(k_fd_xfwd<T, N, F>, smem);
+    cudaError_t e = prep_smem(k_fd_xfwd<T, N, F, CP>, smem);
     if (e != cudaSuccess) return e;
-    k_fd_xfwd<T, N, F><<<dim3((a.g.nz + C - 1) / C, nb), NT, smem, s>>>(a);
+    k_fd_xfwd<T, N, F, CP><<<dim3((a.g.nz + C - 1) / C, nb), NT, smem, s>>>(a);
     return cudaGetLastError();
   }
+}
+
+template <typename T, int N, int F>
+cudaError_t launch_fd_xfwd(const FdXfArgs& a, int nb, cudaStream_t s) {
+  using K = FdCps<T, N>;
+  const int cp = K::xfwd(a.g.nz, nb);
+  if (cp == K::c2) return launch_fd_xfwd_cp<T, N, F, K::c2>(a, nb, s);
+  if (cp == K::c1) return launch_fd_xfwd_cp<T, N, F, K::c1>(a, nb, s);
+  return launch_fd_xfwd_cp<T, N, F, K::c0>(a, nb, s);
 }
 
 struct FdLaunchers {

@@ -195,3 +195,34 @@ def test_group_rejects_shared_plans(cuda):
     b = Ensemble(kh_params(64, 64), [FieldSpec(1e-3)], 3)
     with pytest.raises(ValueError):
         EnsembleGroup([a, b])
+
+
+@pytest.mark.parametrize("precision", ["double", "split"])
+def test_dirichlet_member_bits_independent_of_batch_size(cuda, precision):
+    """The Dirichlet-grid x-forward pass narrows its tile (column pairs per
+    CTA) when a launch is small.  A member's arithmetic does not depend on
+    the tile: one run alone (a quarter-width tile) and the same run inside a
+    160-member batch (the full tile) are bit-identical."""
+    import melvin
+    from melvin import _native as N
+    from melvin.ensemble import Ensemble, FieldSpec
+    from melvin.workloads import conductive
+
+    p = melvin.Parameters({"nx": 64, "nz": 65, "lx": 2.0, "lz": 1.0, "final_time": 1.0, "initial_dt": 1e-6,
+                           "discretisation": ["spectral", "fdm"], "integrator": "explicit", "precision": precision,
+                           "device": "cuda:0"})
+    Pr, RaT = 7.0, 1e5
+    fields = [FieldSpec(Pr, [(1, "ddx", -Pr * RaT), (2, "ddx", Pr * RaT / 2.0)], N.BC_DIRICHLET_W),
+              FieldSpec(1.0, [], N.BC_DIRICHLET_T), FieldSpec(0.01, [], N.BC_DIRICHLET_T)]
+    ic = [np.zeros((64, 65)), conductive(64, 65, 2.0, 1.0, seed=1), conductive(64, 65, 2.0, 1.0, seed=2)]
+    alone = Ensemble(p, fields, 1)
+    alone.load_physical(0, ic)
+    batch = Ensemble(p, fields, 160)
+    for b in range(160):
+        batch.load_physical(b, ic if b == 0 else [np.zeros((64, 65)), conductive(64, 65, 2.0, 1.0, seed=10 + b),
+                                                  conductive(64, 65, 2.0, 1.0, seed=400 + b)])
+    for _ in range(6):
+        alone.step(1e-6)
+        batch.step(1e-6)
+    assert torch.equal(alone.q[0], batch.q[0])
+    assert torch.equal(alone.hist[0], batch.hist[0])
