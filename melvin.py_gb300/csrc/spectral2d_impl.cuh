@@ -365,11 +365,44 @@ struct ZzLayout {
   static_assert(SmemLayout<T, value>::CS >= C0, "z-pass stride below the column count");
 };
 
+// One advected field, one row pair, FP32: the outputs (2 columns) get a
+// layout of their own in the same buffer instead of the inputs' stride 3.
+// The products phase writes them compacted over the inputs, one block of NT
+// rows at a time, behind a barrier (a block's outputs end below the next
+// block's inputs), so the forward FFT and its first-pass scatter run on a
+// stride-2 layout.  Modelled shared-memory wavefronts per CTA at N = 2048:
+// 10670 -> 7422 with radix 16, 10414 -> 8194 with radix 8.
+template <typename T, int F, int P, int RM>
+struct ZzIo {
+  static constexpr bool compact = F == 1 && P == 1 && std::is_same<T, float>::value;
+  static constexpr int in = compact ? ExplicitLayout<3, RM == 16 ? 2 : 0>::value : ZzLayout<T, F, P>::value;
+  static constexpr int out = compact ? ExplicitLayout<2, 1>::value : in;
+};
+
+// The compacted outputs of every block of NT rows end below the inputs of
+// the next block.
+template <typename T, int N, int LI, int LO, int NIN, int NOUT>
+__host__ __device__ constexpr bool zz_compact_safe() {
+  using I = SmemLayout<T, LI>;
+  using O = SmemLayout<T, LO>;
+  for (int z0 = NT; z0 < N; z0 += NT) {
+    const int out_end = (z0 - 1) * O::CS + (NOUT - 1) + ((z0 - 1) >> 3) * O::PAD;
+    const int in_start = z0 * I::CS + (z0 >> 3) * I::PAD;
+    if (out_end >= in_start) return false;
+  }
+  return true;
+}
+
 template <typename T, int N, int F, int P, int RM>
-__global__ void __launch_bounds__(NT, (Occ<T, N, sbuf_elems<T, ZzLayout<T, F, P>::value>(N) * sizeof(cx<T>)>::value))
+__global__ void __launch_bounds__(NT, (Occ<T, N, sbuf_elems<T, ZzIo<T, F, P, RM>::in>(N) * sizeof(cx<T>)>::value))
     k_zz_step(const ZzArgs a) {
   if (gate_closed(a.b.gate)) return;
-  constexpr int NIN = ZzShape<F, P>::NIN, NOUT = ZzShape<F, P>::NOUT, CS = ZzLayout<T, F, P>::value;
+  constexpr int NIN = ZzShape<F, P>::NIN, NOUT = ZzShape<F, P>::NOUT;
+  constexpr int CS = ZzIo<T, F, P, RM>::in, CSO = ZzIo<T, F, P, RM>::out;
+  constexpr bool compact = ZzIo<T, F, P, RM>::compact;
+  static_assert(!compact || (sbuf_elems<T, CSO>(N) <= sbuf_elems<T, CS>(N) &&
+                             zz_compact_safe<T, N, CS, CSO, P * NIN, P * NOUT>()),
+                "compacted z-pass outputs must stay inside the buffer, below later inputs");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* buf = reinterpret_cast<cx<T>*>(smem_raw);
   const GridC& g = a.g;
@@ -402,10 +435,15 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, sbuf_elems<T, ZzLayout<T, F, P>
   block_fft<T, N, P * NIN, CS, NT, +1, RM>(buf, (const cx<T>*)a.tw);
 
   double ke = 0.0, mx = -INFINITY, mz = -INFINITY;
-  for (int z = threadIdx.x; z < N; z += NT) {
+  for (int z0 = 0; z0 < N; z0 += NT) {
+    const int z = z0 + threadIdx.x;
     cx<T> w[P * NIN];
+    if (z < N) {
 #pragma unroll
-    for (int c = 0; c < P * NIN; ++c) w[c] = buf[sx<T, CS>(z, c)];
+      for (int c = 0; c < P * NIN; ++c) w[c] = buf[sx<T, CS>(z, c)];
+    }
+    if constexpr (compact) __syncthreads();  // the block's inputs are read before outputs overwrite them
+    if (z >= N) continue;
 #pragma unroll
     for (int p = 0; p < P; ++p) {
       const cx<T>* wp = w + p * NIN;
@@ -426,14 +464,14 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, sbuf_elems<T, ZzLayout<T, F, P>
 #pragma unroll
       for (int f = 0; f < F; ++f) {
         const T q0 = wp[2 + f].x, q1 = wp[2 + f].y;
-        buf[sx<T, CS>(z, p * NOUT + f)] = mk(ux0 * q0, uz0 * q0);
-        buf[sx<T, CS>(z, p * NOUT + F + f)] = mk(ux1 * q1, uz1 * q1);
+        buf[sx<T, CSO>(z, p * NOUT + f)] = mk(ux0 * q0, uz0 * q0);
+        buf[sx<T, CSO>(z, p * NOUT + F + f)] = mk(ux1 * q1, uz1 * q1);
       }
     }
   }
   __syncthreads();
-  fd_imag_columns<T, N, CS, P * NOUT>(buf, g.sdo, (T)a.fdz);
-  block_fft<T, N, P * NOUT, CS, NT, -1, RM>(buf, (const cx<T>*)a.tw);
+  fd_imag_columns<T, N, CSO, P * NOUT>(buf, g.sdo, (T)a.fdz);
+  block_fft<T, N, P * NOUT, CSO, NT, -1, RM>(buf, (const cx<T>*)a.tw);
   for (int m = threadIdx.x; m < nm; m += NT) {
 #pragma unroll
     for (int p = 0; p < P; ++p) {
@@ -445,7 +483,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, sbuf_elems<T, ZzLayout<T, F, P>
 #pragma unroll
         for (int rho = 0; rho < 2; ++rho) {
           cx<T> A, Cc;
-          get_pair<T, N, CS>(buf, p * NOUT + rho * F + f, m, A, Cc);
+          get_pair<T, N, CSO>(buf, p * NOUT + rho * F + f, m, A, Cc);
           ao[(rho ? r1 : r0) + m] = A;
           co[(rho ? r1 : r0) + m] = Cc;
         }
@@ -861,7 +899,7 @@ cudaError_t launch_xinv(const XinvArgs& a, int njobs, int nb, cudaStream_t s) {
 template <typename T, int N, int F, int V>
 cudaError_t launch_zz_step(const ZzArgs& a, int nb, cudaStream_t s) {
   constexpr int P = ZVar<V>::P, RM = ZVar<V>::RM;
-  const size_t smem = (size_t)sbuf_elems<T, ZzLayout<T, F, P>::value>(N) * sizeof(cx<T>);
+  const size_t smem = (size_t)sbuf_elems<T, ZzIo<T, F, P, RM>::in>(N) * sizeof(cx<T>);
   cudaError_t e = prep_smem(k_zz_step<T, N, F, P, RM>, smem);
   if (e != cudaSuccess) return e;
   k_zz_step<T, N, F, P, RM><<<dim3(a.g.nx / (2 * P), nb), NT, smem, s>>>(a);
@@ -954,7 +992,7 @@ void fill_xinv(FsLaunchers& L, int prec) {
 template <typename T, int N, int F, int V>
 void fill_zz(FsLaunchers& L, int prec) {
   constexpr int P = ZVar<V>::P;
-  constexpr size_t smem = (size_t)sbuf_elems<T, ZzLayout<T, F, P>::value>(N) * sizeof(cx<T>);
+  constexpr size_t smem = (size_t)sbuf_elems<T, ZzIo<T, F, P, ZVar<V>::RM>::in>(N) * sizeof(cx<T>);
   L.zz_shape[prec][F - 1][V] = TileShape{P, ZVar<V>::RM, smem <= kMaxDynSmem ? smem : 0};
   if constexpr (smem <= kMaxDynSmem) {
     L.zz_step[prec][F - 1][V] = launch_zz_step<T, N, F, V>;
