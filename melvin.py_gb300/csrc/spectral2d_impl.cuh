@@ -393,8 +393,20 @@ __host__ __device__ constexpr bool zz_compact_safe() {
   return true;
 }
 
+// Resident CTAs the z pass asks for.  The FP64 pass with one field and one
+// row pair takes two where its shared memory allows (128 registers; a few
+// hundred bytes spill to L1, which this FP64-bound kernel leaves idle): at
+// 2048 points 0.780 -> 0.761 ms.  With more fields the spills grow to
+// kilobytes, so those keep Occ.
 template <typename T, int N, int F, int P, int RM>
-__global__ void __launch_bounds__(NT, (Occ<T, N, sbuf_elems<T, ZzIo<T, F, P, RM>::in>(N) * sizeof(cx<T>)>::value))
+struct ZzOcc {
+  using O = Occ<T, N, sbuf_elems<T, ZzIo<T, F, P, RM>::in>(N) * sizeof(cx<T>)>;
+  static constexpr bool two = std::is_same<T, double>::value && F == 1 && P == 1 && O::by_smem >= 2;
+  static constexpr int value = two ? 2 : O::value;
+};
+
+template <typename T, int N, int F, int P, int RM>
+__global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
     k_zz_step(const ZzArgs a) {
   if (gate_closed(a.b.gate)) return;
   constexpr int NIN = ZzShape<F, P>::NIN, NOUT = ZzShape<F, P>::NOUT;
