@@ -253,6 +253,9 @@ typedef struct mgb_equation {
   int32_t order;       /* integrator_order: 2 or 4 */
   double alpha;        /* semi-implicit alpha (Parameters.alpha = 0.51) */
   mgb_field_eq f[3];
+  int32_t diag_flux;   /* 0: three diagnostics; k in 1..nfields: a fourth, the convective flux
+                          mean(uz * q) of field k-1 in physical space (the Nusselt number of
+                          examples/double_diffusive_convection.py:20-23 is 1 minus it) */
 } mgb_equation;
 
 /* Compute into `work` the per-mode update coefficients of `eq` at `dt`
@@ -269,8 +272,9 @@ int mgb_step_prepare(const mgb_plan* plan, const mgb_equation* eq, double dt, vo
  * kernels.  q[f]: spectral states (updated in place); hist[f]: histories;
  * `curr` is the history slot that receives this step's derivative (the
  * caller advances it afterwards, as TimeDerivative.advance does).  `diag`
- * (device, 3 doubles, may be NULL) receives kinetic energy, max ux, max uz
- * of the velocity at the start of the step. */
+ * (device, 3 doubles, or 4 when eq->diag_flux is set; may be NULL)
+ * receives kinetic energy, max ux, max uz of the velocity at the start of
+ * the step, and the convective flux eq->diag_flux asks for. */
 int mgb_step(const mgb_plan* plan, const mgb_equation* eq, void* const* q, void* const* hist,
              int32_t curr, double dt, void* work, double* diag, void* stream);
 
@@ -297,8 +301,9 @@ typedef struct mgb_batch {
 int mgb_batch_workspace_bytes(const mgb_plan* plan, int32_t nfields, int32_t count, size_t* bytes);
 /* mgb_step for a batch: one call advances every listed member by one step
  * (same equation, dt and curr for all; mgb_step_prepare on the same
- * workspace first).  `diag` (device, count x 3 doubles, may be NULL)
- * receives each member's kinetic energy, max ux, max uz. */
+ * workspace first).  `diag` (device, count x 3 doubles, or count x 4
+ * with eq->diag_flux; may be NULL) receives each member's diagnostics as
+ * mgb_step does. */
 int mgb_batch_step(const mgb_plan* plan, const mgb_equation* eq, const mgb_batch* batch, int32_t curr,
                    double dt, void* work, double* diag, void* stream);
 
@@ -348,7 +353,8 @@ typedef struct mgb_run_state {   /* device memory, filled by the caller before m
   int32_t dt_changed;      /* the last tick shrank dt (coefficients are refreshed) */
   int32_t ntracked;        /* tracker samples written */
   int32_t dropped;         /* tracker samples that found the buffer full */
-  double diag[3];          /* kinetic energy, max ux, max uz of the last diagnosed step */
+  double diag[4];          /* kinetic energy, max ux, max uz of the last diagnosed step, and the
+                              convective flux when eq->diag_flux is set */
 } mgb_run_state;
 
 typedef struct mgb_run_config {  /* host memory */
@@ -362,6 +368,9 @@ typedef struct mgb_run_config {  /* host memory */
                               save time of the time-based tickers; +inf for none) */
   double* tracker_t;       /* device [capacity]: t of each sample */
   double* tracker_ke;      /* device [capacity]: kinetic energy (calc_kinetic_energy, melvin/utility.py:42-59) */
+  double* tracker_flux;    /* device [capacity] or NULL: the convective flux of eq->diag_flux at
+                              each sample (1 minus the Nusselt number of
+                              examples/double_diffusive_convection.py:20-23) */
 } mgb_run_config;
 
 #define MGB_RUN_TICK 1   /* tick after this iteration (end_loop, stop point) */

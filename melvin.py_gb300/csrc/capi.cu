@@ -240,7 +240,7 @@ int mgb_plan_shapes(const mgb_plan* p, int32_t* spec_rows, int32_t* spec_cols, i
 int mgb_workspace_bytes(const mgb_plan* p, int32_t family, int32_t nfields, size_t* bytes) {
   CHECK_PLAN(p);
   CHECK_PTR(bytes);
-  const size_t diag = 152 * 4 * 3 * sizeof(double) + 256;
+  const size_t diag = 152 * 4 * kDiagW * sizeof(double) + 256;
   if (family == 0) {
     size_t b = p->g.fdm ? fd_verb_workspace(p) : 2 * inter_bytes(p->g, MGB_PREC_DOUBLE);
     *bytes = (b > diag ? b : diag) + 256;
@@ -429,6 +429,8 @@ static int check_equation(const mgb_equation* eq, int32_t curr) {
   if (F < 1 || F > 3) return fail(MGB_ERR_INVALID, "nfields=%d (1..3)", F);
   if (eq->order != 2 && eq->order != 4) return fail(MGB_ERR_INVALID, "integrator_order=%d (2 or 4)", eq->order);
   if (curr < 0 || curr >= eq->order) return fail(MGB_ERR_INVALID, "curr_idx=%d out of range", curr);
+  if (eq->diag_flux < 0 || eq->diag_flux > F)
+    return fail(MGB_ERR_INVALID, "diag_flux=%d (0 for none, or 1..nfields)", eq->diag_flux);
   for (int f = 0; f < F; ++f) {
     const mgb_field_eq& fe = eq->f[f];
     if (fe.nterms < 0 || fe.nterms > 4) return fail(MGB_ERR_INVALID, "field %d: nterms=%d (0..4)", f, fe.nterms);
@@ -594,6 +596,8 @@ int mgb_run_step(const mgb_plan* p, const mgb_equation* eq, void* const* q, void
     return fail(MGB_ERR_INVALID, "%s: CFL tick without a CFL cadence", __func__);
   if ((flags & MGB_RUN_TRACK) && cfg->tracker_cadence < 1)
     return fail(MGB_ERR_INVALID, "%s: tracker tick without a tracker cadence", __func__);
+  if (cfg->tracker_flux && !eq->diag_flux)
+    return fail(MGB_ERR_INVALID, "%s: a flux tracker needs eq->diag_flux", __func__);
   double dt = 0.0;
   if (!p->g.fdm) {
     std::lock_guard<std::mutex> lock(p->mu);

@@ -16,6 +16,7 @@ struct TickArgs {
   int flags, cfl_cadence, tracker_cadence, capacity;
   double* tracker_t;
   double* tracker_ke;
+  double* tracker_flux;  // or null
 };
 
 // Python's builtin min(a, b) as the reference calls it: `b` when b < a,
@@ -56,6 +57,7 @@ __global__ void k_run_tick(mgb_run_state* st, TickArgs a) {
     if (st->ntracked < a.capacity) {
       a.tracker_t[st->ntracked] = st->t;
       a.tracker_ke[st->ntracked] = st->diag[0];
+      if (a.tracker_flux) a.tracker_flux[st->ntracked] = st->diag[3];
       st->ntracked += 1;
     } else {
       st->dropped += 1;
@@ -99,6 +101,7 @@ int run_tick(const mgb_plan* p, mgb_run_state* st, const mgb_run_config* cfg, lo
   a.capacity = cfg->capacity;
   a.tracker_t = cfg->tracker_t;
   a.tracker_ke = cfg->tracker_ke;
+  a.tracker_flux = cfg->tracker_flux;
   k_run_tick<<<1, 32, 0, s>>>(st, a);
   MGB_LAUNCH_CHECK();
   return MGB_OK;

@@ -253,7 +253,7 @@ static FdWork fd_carve(const mgb_plan* p, int F, void* base) {
     off += S;
   }
   w.partial = off;
-  off += align256((size_t)nctas * 3 * sizeof(double));
+  off += align256((size_t)nctas * kDiagW * sizeof(double));
   w.member_bytes = off;
   w.base = (char*)base;
   return w;
@@ -311,6 +311,7 @@ static int fd_stage(const mgb_plan* p, const mgb_equation* eq, const FdWork& w, 
   }
   pa.nf = F;
   pa.partial = diag ? wmp(w, w.partial) : mp(nullptr);
+  pa.flux_f = eq->diag_flux - 1;
   pa.fdx = fd_inv(g.sdo, g.dx);
   pa.fdz = fd_inv(g.sdo, g.dz);
   pa.gate = sb.gate;
@@ -389,8 +390,9 @@ int fd_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
   if (diag) {
     // per-member partials sit member_bytes apart: fold each member's block
     for (int z = 0; z < sb.count; ++z) {
+      const int ow = eq->diag_flux ? 4 : 3;
       st = pw_finish_diag((const double*)(w.base + (size_t)z * w.member_bytes + w.partial), nctas, 1,
-                          1.0 / ((double)g.nx * (double)g.nz), diag + 3 * z, s);
+                          1.0 / ((double)g.nx * (double)g.nz), diag + ow * z, s, ow);
       if (st) return st;
     }
   }

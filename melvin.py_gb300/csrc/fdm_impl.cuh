@@ -416,8 +416,10 @@ struct FdPhysArgs {
   Mptr uz;
   Mptr q[3];
   Mptr jout[3];
-  Mptr partial;      // optional (base null): per-CTA diagnostics (sum ux^2+uz^2, max ux, max uz)
+  Mptr partial;      // optional (base null): per-CTA diagnostics (sum ux^2+uz^2, max ux, max uz,
+                     // sum uz*q of field flux_f)
   int nf;
+  int flux_f;        // -1: none
   double fdx, fdz;   // 1/(2dx) or 1/(3dx); same for z
   Gate gate;
 };
@@ -455,7 +457,7 @@ __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
     s_uz[i][k] = (x < nx && z >= 0 && z < nz) ? uz[(size_t)x * nz + z] : (T)0;
   }
   __syncthreads();
-  double ke = 0, mx = -INFINITY, mz = -INFINITY;
+  double ke = 0, mx = -INFINITY, mz = -INFINITY, fl = 0;
   if (a.partial.base) {
     for (int e = threadIdx.x; e < FD_TX * FD_TZ; e += NT) {
       const int i = e / FD_TZ, k = e - i * FD_TZ;
@@ -475,6 +477,12 @@ __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
       s_q[i][k] = (z >= 0 && z < nz) ? q[(size_t)x * nz + z] : (T)0;
     }
     __syncthreads();
+    if (a.partial.base && f == a.flux_f) {
+      for (int e = threadIdx.x; e < FD_TX * FD_TZ; e += NT) {
+        const int i = e / FD_TZ, k = e - i * FD_TZ;
+        if (x0 + i < nx && z0 + k < nz) fl += (double)s_uz[i][k + H] * (double)s_q[i + H][k + H];
+      }
+    }
     T* jo = (T*)maddr(a.jout[f], nullptr, blockIdx.z);
     for (int e = threadIdx.x; e < FD_TX * FD_TZ; e += NT) {
       const int i = e / FD_TZ, k = e - i * FD_TZ;
@@ -492,9 +500,10 @@ __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
     __syncthreads();
   }
   if (a.partial.base) {
-    __shared__ double red[3][NT / 32];
+    __shared__ double red[4][NT / 32];
     for (int o = 16; o > 0; o >>= 1) {
       ke += __shfl_xor_sync(0xffffffffu, ke, o);
+      fl += __shfl_xor_sync(0xffffffffu, fl, o);
       const double t1 = __shfl_xor_sync(0xffffffffu, mx, o), t2 = __shfl_xor_sync(0xffffffffu, mz, o);
       mx = (t1 != t1 || t1 > mx) ? t1 : mx;
       mz = (t2 != t2 || t2 > mz) ? t2 : mz;
@@ -503,20 +512,23 @@ __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
       red[0][threadIdx.x >> 5] = ke;
       red[1][threadIdx.x >> 5] = mx;
       red[2][threadIdx.x >> 5] = mz;
+      red[3][threadIdx.x >> 5] = fl;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-      double S = 0, MX = -INFINITY, MZ = -INFINITY;
+      double S = 0, MX = -INFINITY, MZ = -INFINITY, FL = 0;
       for (int i = 0; i < NT / 32; ++i) {
         S += red[0][i];
+        FL += red[3][i];
         MX = (red[1][i] != red[1][i] || red[1][i] > MX) ? red[1][i] : MX;
         MZ = (red[2][i] != red[2][i] || red[2][i] > MZ) ? red[2][i] : MZ;
       }
       const int cta = blockIdx.y * gridDim.x + blockIdx.x;
       double* part = (double*)maddr(a.partial, nullptr, blockIdx.z);
-      part[3 * cta + 0] = S;
-      part[3 * cta + 1] = MX;
-      part[3 * cta + 2] = MZ;
+      part[kDiagW * cta + 0] = S;
+      part[kDiagW * cta + 1] = MX;
+      part[kDiagW * cta + 2] = MZ;
+      part[kDiagW * cta + 3] = FL;
     }
   }
 }

@@ -174,6 +174,11 @@ int pw_diagnostics(const mgb_plan* p, const double* ux, const double* uz, double
                    cudaStream_t s);
 // Fold per-CTA partials [count][n][3] (sum, max, max) into
 // out[count][3] = {0.5*sum/(nx*nz), max, max}.
-int pw_finish_diag(const double* partial, int n, int count, double inv_npts, double* out, cudaStream_t s);
+// Per-CTA diagnostics partials are kDiagW doubles: sum of ux^2 + uz^2, max ux,
+// max uz, sum of uz * q for the flux field (0 when none).  The fold writes
+// ow = 3 or 4 values per member.
+constexpr int kDiagW = 4;
+int pw_finish_diag(const double* partial, int n, int count, double inv_npts, double* out, cudaStream_t s,
+                   int ow = 3);
 
 }  // namespace mgb

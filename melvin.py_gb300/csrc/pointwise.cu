@@ -228,31 +228,36 @@ __global__ void k_adams(size_t total, int corrector, const zd* __restrict__ hist
 __device__ __forceinline__ double nmax(double m, double v) { return (v != v || v > m) ? v : m; }
 
 template <int THREADS>
-__device__ __forceinline__ void reduce3(double& s, double& mx, double& mz) {
-  __shared__ double red[3][THREADS / 32];
+__device__ __forceinline__ void reduce4(double& s, double& mx, double& mz, double& fl) {
+  __shared__ double red[4][THREADS / 32];
   for (int o = 16; o > 0; o >>= 1) {
     s += __shfl_xor_sync(0xffffffffu, s, o);
     mx = nmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     mz = nmax(mz, __shfl_xor_sync(0xffffffffu, mz, o));
+    fl += __shfl_xor_sync(0xffffffffu, fl, o);
   }
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   if (l == 0) {
     red[0][w] = s;
     red[1][w] = mx;
     red[2][w] = mz;
+    red[3][w] = fl;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     s = 0;
     mx = -INFINITY;
     mz = -INFINITY;
+    fl = 0;
     for (int i = 0; i < THREADS / 32; ++i) {
       s += red[0][i];
       mx = nmax(mx, red[1][i]);
       mz = nmax(mz, red[2][i]);
+      fl += red[3][i];
     }
   }
 }
+
 
 // Per-CTA partial sums of ux^2 + uz^2 and signed maxima (fixed assignment
 // of elements to CTAs, so the result does not depend on scheduling).
@@ -265,28 +270,36 @@ __global__ void k_diag_partial(size_t total, const double* __restrict__ ux, cons
     mx = nmax(mx, a);
     mz = nmax(mz, b);
   }
-  reduce3<PT>(s, mx, mz);
+  double fl = 0;
+  reduce4<PT>(s, mx, mz, fl);
   if (threadIdx.x == 0) {
-    partial[3 * blockIdx.x + 0] = s;
-    partial[3 * blockIdx.x + 1] = mx;
-    partial[3 * blockIdx.x + 2] = mz;
+    partial[kDiagW * blockIdx.x + 0] = s;
+    partial[kDiagW * blockIdx.x + 1] = mx;
+    partial[kDiagW * blockIdx.x + 2] = mz;
+    partial[kDiagW * blockIdx.x + 3] = fl;
   }
 }
 
-__global__ void k_diag_finish(const double* __restrict__ partial, int n, double inv_npts, double* __restrict__ out) {
-  partial += (size_t)blockIdx.x * n * 3;
-  out += (size_t)blockIdx.x * 3;
-  double s = 0, mx = -INFINITY, mz = -INFINITY;
+// Per member (blockIdx.x): fold n partials into kinetic energy
+// (calc_kinetic_energy, melvin/utility.py:42-59), max ux, max uz and, for
+// ow = 4, the mean convective flux.
+__global__ void k_diag_finish(const double* __restrict__ partial, int n, double inv_npts, int ow,
+                              double* __restrict__ out) {
+  partial += (size_t)blockIdx.x * n * kDiagW;
+  out += (size_t)blockIdx.x * ow;
+  double s = 0, mx = -INFINITY, mz = -INFINITY, fl = 0;
   for (int i = threadIdx.x; i < n; i += PT) {
-    s += partial[3 * i];
-    mx = nmax(mx, partial[3 * i + 1]);
-    mz = nmax(mz, partial[3 * i + 2]);
+    s += partial[kDiagW * i];
+    mx = nmax(mx, partial[kDiagW * i + 1]);
+    mz = nmax(mz, partial[kDiagW * i + 2]);
+    fl += partial[kDiagW * i + 3];
   }
-  reduce3<PT>(s, mx, mz);
+  reduce4<PT>(s, mx, mz, fl);
   if (threadIdx.x == 0) {
     out[0] = 0.5 * s * inv_npts;
     out[1] = mx;
     out[2] = mz;
+    if (ow == 4) out[3] = fl * inv_npts;
   }
 }
 
@@ -405,8 +418,8 @@ int pw_adams(const mgb_plan* p, int corrector, const zd* hist, int order, int cu
   return MGB_OK;
 }
 
-int pw_finish_diag(const double* partial, int n, int count, double inv_npts, double* out, cudaStream_t s) {
-  k_diag_finish<<<count, PT, 0, s>>>(partial, n, inv_npts, out);
+int pw_finish_diag(const double* partial, int n, int count, double inv_npts, double* out, cudaStream_t s, int ow) {
+  k_diag_finish<<<count, PT, 0, s>>>(partial, n, inv_npts, ow, out);
   MGB_LAUNCH_CHECK();
   return MGB_OK;
 }

@@ -173,7 +173,7 @@ static inline size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 // and the transform intermediates.
 struct FsWork {
   zd* coef[3];
-  double* partial;        // [count][nx/2][3]
+  double* partial;        // [count][nx/2][kDiagW]
   char* inter[6];         // member 0's intermediates
   size_t inter_stride;    // bytes between members' intermediate blocks
   size_t bytes;
@@ -191,7 +191,7 @@ static FsWork fs_carve(const mgb_plan* p, int F, int count, void* base) {
     if (f < F) off += al256((size_t)p->g.rows * p->g.cols * sizeof(zd));
   }
   w.partial = (double*)(c + off);
-  off += al256((size_t)count * (p->g.nx / 2) * 3 * sizeof(double));
+  off += al256((size_t)count * (p->g.nx / 2) * kDiagW * sizeof(double));
   for (int i = 0; i < 6; ++i) w.inter[i] = c + off + (size_t)(i < ninter ? i : ninter - 1) * ib;
   w.inter_stride = (size_t)ninter * ib;
   off += (size_t)count * w.inter_stride;
@@ -342,6 +342,7 @@ int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
     za.cout[f] = w.inter[F + f];
   }
   za.partial = diag ? w.partial : nullptr;
+  za.flux_f = eq->diag_flux - 1;
   za.fdz = fd_inv(g.sdo, g.dz);
   za.tw = twz;
   st = launched(Lz->zz_step[prec][F - 1][tile[MGB_FAMILY_ZSTEP]](za, nb, s), "step z pass");
@@ -381,7 +382,8 @@ int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
   et->mark(s);
   if (diag) {
     const int pairs = Lz->zz_shape[prec][F - 1][tile[MGB_FAMILY_ZSTEP]].shape;
-    return pw_finish_diag(w.partial, g.nx / (2 * pairs), nb, 1.0 / ((double)g.nx * (double)g.nz), diag, s);
+    return pw_finish_diag(w.partial, g.nx / (2 * pairs), nb, 1.0 / ((double)g.nx * (double)g.nz), diag, s,
+                          eq->diag_flux ? 4 : 3);
   }
   return MGB_OK;
 }

@@ -282,31 +282,35 @@ __device__ __forceinline__ void fd_imag_columns(cx<T>* buf, int sdo, T inv) {
   __syncthreads();
 }
 
-// Deterministic CTA reduction of (sum, max, max) -> partial[blockIdx.x*3].
-__device__ __forceinline__ void block_diag(double s, double mx, double mz, double* partial) {
-  __shared__ double red[3][NT / 32];
+// Deterministic CTA reduction of (sum, max, max, sum) -> partial[blockIdx.x*kDiagW].
+__device__ __forceinline__ void block_diag(double s, double mx, double mz, double fl, double* partial) {
+  __shared__ double red[4][NT / 32];
   for (int o = 16; o > 0; o >>= 1) {
     s += __shfl_xor_sync(0xffffffffu, s, o);
     mx = nan_max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     mz = nan_max(mz, __shfl_xor_sync(0xffffffffu, mz, o));
+    fl += __shfl_xor_sync(0xffffffffu, fl, o);
   }
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   if (l == 0) {
     red[0][w] = s;
     red[1][w] = mx;
     red[2][w] = mz;
+    red[3][w] = fl;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double S = 0, MX = -INFINITY, MZ = -INFINITY;
+    double S = 0, MX = -INFINITY, MZ = -INFINITY, FL = 0;
     for (int i = 0; i < NT / 32; ++i) {
       S += red[0][i];
       MX = nan_max(MX, red[1][i]);
       MZ = nan_max(MZ, red[2][i]);
+      FL += red[3][i];
     }
-    partial[3 * blockIdx.x + 0] = S;
-    partial[3 * blockIdx.x + 1] = MX;
-    partial[3 * blockIdx.x + 2] = MZ;
+    partial[kDiagW * blockIdx.x + 0] = S;
+    partial[kDiagW * blockIdx.x + 1] = MX;
+    partial[kDiagW * blockIdx.x + 2] = MZ;
+    partial[kDiagW * blockIdx.x + 3] = FL;
   }
 }
 
@@ -330,7 +334,8 @@ struct ZzArgs {
   void* cout[3];
   double* ux_phys;    // optional physical velocity
   double* uz_phys;
-  double* partial;    // optional [member][gridDim.x][3]
+  double* partial;    // optional [member][gridDim.x][kDiagW]
+  int flux_f;         // field whose sum of uz * q the partials carry (-1: none)
   double fdz;         // 1/(2dz) or 1/(3dz)
   const void* tw;
   BatchC b;           // member = blockIdx.y
@@ -446,7 +451,7 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
   __syncthreads();
   block_fft<T, N, P * NIN, CS, NT, +1, RM>(buf, (const cx<T>*)a.tw);
 
-  double ke = 0.0, mx = -INFINITY, mz = -INFINITY;
+  double ke = 0.0, mx = -INFINITY, mz = -INFINITY, fl = 0.0;
   for (int z0 = 0; z0 < N; z0 += NT) {
     const int z = z0 + threadIdx.x;
     cx<T> w[P * NIN];
@@ -476,6 +481,7 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
 #pragma unroll
       for (int f = 0; f < F; ++f) {
         const T q0 = wp[2 + f].x, q1 = wp[2 + f].y;
+        if (a.partial && f == a.flux_f) fl += (double)uz0 * (double)q0 + (double)uz1 * (double)q1;
         buf[sx<T, CSO>(z, p * NOUT + f)] = mk(ux0 * q0, uz0 * q0);
         buf[sx<T, CSO>(z, p * NOUT + F + f)] = mk(ux1 * q1, uz1 * q1);
       }
@@ -502,7 +508,7 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
       }
     }
   }
-  if (a.partial) block_diag(ke, mx, mz, a.partial + (size_t)blockIdx.y * gridDim.x * 3);
+  if (a.partial) block_diag(ke, mx, mz, fl, a.partial + (size_t)blockIdx.y * gridDim.x * kDiagW);
 }
 
 // ---------------------------------------------------------------------------

@@ -113,7 +113,7 @@ class MgbRunState(C.Structure):
         ("dt_changed", C.c_int32),
         ("ntracked", C.c_int32),
         ("dropped", C.c_int32),
-        ("diag", C.c_double * 3),
+        ("diag", C.c_double * 4),
     ]
 
 
@@ -128,6 +128,7 @@ class MgbRunConfig(C.Structure):
         ("pause_time", C.c_double),
         ("tracker_t", C.c_void_p),
         ("tracker_ke", C.c_void_p),
+        ("tracker_flux", C.c_void_p),
     ]
 
 
@@ -147,6 +148,7 @@ class MgbEquation(C.Structure):
         ("order", C.c_int32),
         ("alpha", C.c_double),
         ("f", MgbFieldEq * 3),
+        ("diag_flux", C.c_int32),
     ]
 
 

@@ -10,7 +10,9 @@ and the loop-counted tickers of ``end_loop`` (melvin/Ticker.py:1-35) call
 ``Integrator.set_dt`` every ``cfl_cadence`` loops (a host reduction of the
 velocity and a possible ``Exception("CFL condition breached")``,
 melvin/Integrator.py:35-44) and the scalar trackers every
-``tracker_cadence`` loops (melvin/Simulation.py:86-97).  Each of those reads
+``tracker_cadence`` loops (melvin/Simulation.py:86-97): in the examples the
+kinetic energy (melvin/utility.py:42-59) and the Nusselt number
+(examples/double_diffusive_convection.py:20-23).  Each of those reads
 the device, so the reference synchronises at every check.
 
 :class:`DeviceRun` keeps t, dt, the loop counter, the ticker counters and the
@@ -36,6 +38,8 @@ at the end of a run.
 from __future__ import annotations
 
 import ctypes as C
+import functools
+import os
 
 import numpy as np
 import torch
@@ -52,9 +56,12 @@ class DeviceRun:
                     searched that far ahead)
     capacity        kinetic-energy samples held on the device per segment
 
-    A simulation with scalar trackers must track only "kinetic_energy"
-    (sampled on the device from the step's own velocity); other tracker
-    functions need host arrays and raise ValueError.
+    Scalar trackers are sampled on the device from the step's own
+    start-of-step velocity and fields: the kinetic energy
+    (``calc_kinetic_energy``, or a tracker file named "kinetic_energy") and
+    the Nusselt number 1 - mean(tmp * uz) (``calc_nusselt_number`` of one of
+    the stepper's fields, bound with functools.partial as the examples do).
+    Other tracker functions need host arrays and raise ValueError.
     """
 
     def __init__(self, simulation, stepper, cfl=None, horizon=64, capacity=1 << 16):
@@ -64,16 +71,40 @@ class DeviceRun:
         self.cfl = hasattr(simulation, "_cfl_ticker") if cfl is None else bool(cfl)
         if self.cfl and not hasattr(simulation, "_cfl_ticker"):
             raise ValueError("cfl=True needs simulation.config_cfl(ux, uz) first (as the reference)")
-        names = [t._filename for t in getattr(simulation, "_trackers", [])]
-        if names and names != ["kinetic_energy"]:
-            raise ValueError(f"only a 'kinetic_energy' tracker runs on the device, not {names}")
-        self.track = bool(names)
+        self.kinds, flux = [], None
+        trackers = getattr(simulation, "_trackers", [])
+        fns = getattr(simulation, "_tracker_fns", [None] * len(trackers))
+        for tr, fn in zip(trackers, fns):
+            kind, var = self._classify(tr, fn)
+            if kind == "nusselt":
+                if flux is not None and var is not flux:
+                    raise ValueError("Nusselt trackers of different fields cannot share the device flux")
+                flux = var
+            self.kinds.append(kind)
+        self.track = bool(self.kinds)
+        stepper.set_flux_field(flux)
+        self.flux = flux is not None
         self.horizon = int(horizon)
         self.capacity = int(capacity) if self.track else 0
         self._state = torch.zeros(C.sizeof(N.MgbRunState), dtype=torch.uint8, device=self.device)
         self._host = torch.zeros(C.sizeof(N.MgbRunState), dtype=torch.uint8).pin_memory()
-        self._trk = torch.zeros((2, max(self.capacity, 1)), dtype=torch.float64, device=self.device)
+        self._trk = torch.zeros((3, max(self.capacity, 1)), dtype=torch.float64, device=self.device)
         self.last_state = None
+
+    @staticmethod
+    def _classify(tracker, fn):
+        """("ke", None) or ("nusselt", tmp Variable) for a tracker function."""
+        if isinstance(fn, functools.partial):
+            name = getattr(fn.func, "__name__", "")
+            if name == "calc_kinetic_energy":
+                return "ke", None
+            if name == "calc_nusselt_number" and fn.args:
+                return "nusselt", fn.args[0]
+        stem = os.path.splitext(os.path.basename(tracker._filename))[0]
+        if stem == "kinetic_energy":
+            return "ke", None
+        raise ValueError(f"tracker {tracker._filename!r}: only the kinetic energy and the Nusselt number "
+                         "(calc_nusselt_number bound to a stepped field) run on the device")
 
     # -- state transfer -------------------------------------------------
 
@@ -138,6 +169,7 @@ class DeviceRun:
         cfg.pause_time = float(min(timed)) if timed else float("inf")
         cfg.tracker_t = self._trk[0].data_ptr()
         cfg.tracker_ke = self._trk[1].data_ptr()
+        cfg.tracker_flux = self._trk[2].data_ptr() if self.flux else None
 
         st_.prepare(s0.dt)
         self.plan.last_prepared = st_
@@ -197,9 +229,10 @@ class DeviceRun:
             n = int(s.ntracked)
             if n:
                 tv = self._trk[:, :n].cpu().numpy()
-                tracker = sim._trackers[0]
-                for t, v in zip(tv[0], tv[1]):
-                    tracker.append(float(t), np.float64(v))
+                for tracker, kind in zip(sim._trackers, self.kinds):
+                    vals = tv[1] if kind == "ke" else 1.0 - tv[2]
+                    for t, v in zip(tv[0], vals):
+                        tracker.append(float(t), np.float64(v))
             if s.dropped:
                 raise RuntimeError(f"{s.dropped} kinetic-energy samples did not fit the device buffer "
                                    f"(capacity {self.capacity})")

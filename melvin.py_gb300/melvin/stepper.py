@@ -75,10 +75,24 @@ class Stepper:
                 fe.terms[k] = N.MgbTerm(src, OPS[t.op], t.coef)
         self.eq = eq
         self.work = self.plan.step_work(len(fields))
-        self.diag = torch.zeros(3, dtype=torch.float64, device=self.device)
+        self.diag = torch.zeros(4, dtype=torch.float64, device=self.device)
         self._q = (C.c_void_p * 3)()
         self._h = (C.c_void_p * 3)()
         self._prepared_dt = None
+
+    def set_flux_field(self, var):
+        """Make the step's diagnostics carry a fourth value, the convective
+        flux mean(uz * q) of the advected field `var` at the start of the
+        step (None: three values)."""
+        if var is None:
+            self.eq.diag_flux = 0
+            self.diag[3:].zero_()  # nothing writes it from here on
+            return
+        for i, f in enumerate(self.fields):
+            if f.var is var:
+                self.eq.diag_flux = i + 1
+                return
+        raise ValueError("the flux field must be one of the stepper's advected fields")
 
     def prepare(self, dt):
         """(Re)compute the per-mode update coefficients for `dt`."""
@@ -93,8 +107,9 @@ class Stepper:
 
     def step(self, dt=None, diagnostics=False):
         """Advance every field by one step; returns the device tensor
-        (kinetic energy, max ux, max uz) of the start-of-step velocity when
-        `diagnostics` is set."""
+        (kinetic energy, max ux, max uz, convective flux) of the start-of-step
+        velocity when `diagnostics` is set (the flux only after
+        set_flux_field, else 0)."""
         dt = self.sim._integrator._dt if dt is None else dt
         self._ensure(dt)
         curr = self.fields[0].dvar._curr_idx

@@ -43,6 +43,13 @@ def calc_kinetic_energy(ux, uz, xp=None, params=None):
     return float(out[0].item())
 
 
+def calc_nusselt_number(tmp, uz, xp=None, params=None):
+    """``1 - mean(tmp * uz)`` over the physical fields, the tracker of
+    examples/double_diffusive_convection.py:20-23 (after Stellmach et al.
+    2011); returns a Python float."""
+    return float(1.0 - torch.mean(tmp.getp() * uz.getp()).item())
+
+
 def calc_velocity_from_vorticity(vorticity, streamfunction, ux, uz, laplacian_solver=None):
     """psi = solve(-w); ux = -d/dz psi, uz = d/dx psi (melvin/utility.py:62-79).
 

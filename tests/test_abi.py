@@ -66,6 +66,7 @@ def test_ctypes_struct_layout_matches_c(tmp_path):
         " offsetof(mgb_batch, term_coef), sizeof(mgb_tile_info), offsetof(mgb_tile_info, smem_bytes));\n"
         'printf("%zu %zu %zu %zu %zu\\n", sizeof(mgb_run_state), offsetof(mgb_run_state, status),'
         " offsetof(mgb_run_state, diag), sizeof(mgb_run_config), offsetof(mgb_run_config, tracker_ke));\n"
+        'printf("%zu %zu\\n", offsetof(mgb_equation, diag_flux), offsetof(mgb_run_config, tracker_flux));\n'
         "return 0;}\n"
     )
     exe = tmp_path / "layout"
@@ -74,7 +75,8 @@ def test_ctypes_struct_layout_matches_c(tmp_path):
     sizes = list(map(int, out[:4]))
     offs = list(map(int, out[4:8]))
     more = list(map(int, out[8:13]))
-    run = list(map(int, out[13:]))
+    run = list(map(int, out[13:18]))
+    tail = list(map(int, out[18:]))
     assert sizes == [C.sizeof(N.MgbGrid), C.sizeof(N.MgbTerm), C.sizeof(N.MgbFieldEq), C.sizeof(N.MgbEquation)]
     assert offs == [N.MgbGrid.lx.offset, N.MgbGrid.precision.offset, N.MgbFieldEq.terms.offset,
                     N.MgbEquation.f.offset]
@@ -82,3 +84,4 @@ def test_ctypes_struct_layout_matches_c(tmp_path):
                     C.sizeof(N.MgbTileInfo), N.MgbTileInfo.smem_bytes.offset]
     assert run == [C.sizeof(N.MgbRunState), N.MgbRunState.status.offset, N.MgbRunState.diag.offset,
                    C.sizeof(N.MgbRunConfig), N.MgbRunConfig.tracker_ke.offset]
+    assert tail == [N.MgbEquation.diag_flux.offset, N.MgbRunConfig.tracker_flux.offset]

@@ -187,3 +187,122 @@ def test_device_run_split_precision(cuda):
     DeviceRun(b[0], b[1]).run()
     # the fused step's velocity is FP32 here, the host tickers' per-verb one FP64
     compare(a, b, ["w"], ke_rtol=1e-5)
+
+
+# ---- the Nusselt tracker (examples/double_diffusive_convection.py:20-23, 80-89) ----
+
+
+def _ddc_sim(n=64, dt=None, final_time=None, precision="double", fdm=False):
+    """Fully spectral double-diffusive convection (the example's equations
+    and trackers), or Rayleigh-Benard on the Dirichlet grid; both with the
+    kinetic-energy and Nusselt trackers and the CFL check."""
+    import melvin
+    from melvin import BasisFunctions as B, equations, workloads
+    from melvin.utility import calc_kinetic_energy, calc_nusselt_number
+
+    nz = n // 2 + 1 if fdm else n
+    # 250 steps; the Dirichlet grid's explicit diffusion needs dt below ~1.2e-4 at 64x33
+    dt = dt if dt is not None else (2e-5 if fdm else 2e-4)
+    final_time = final_time if final_time is not None else 250 * dt
+    lx, lz = (2.0, 1.0) if fdm else (4.0, 2.0)
+    prm = {"nx": n, "nz": nz, "lx": lx, "lz": lz, "final_time": final_time, "initial_dt": dt, "cfl_cadence": 4,
+           "tracker_cadence": 3, "precision": precision, "device": "cuda:0"}
+    if fdm:
+        prm.update({"discretisation": ["spectral", "fdm"], "integrator": "explicit"})
+    p = melvin.Parameters(prm)
+    sim = melvin.Simulation(p, torch)
+    bf = [B.COMPLEX_EXP, B.FDM if fdm else B.COMPLEX_EXP]
+    names = ("w", "psi", "ux", "uz", "tmp") + (() if fdm else ("xi",))
+    V = {k: sim.make_variable(k, bf) for k in names}
+    D = {k: sim.make_derivative("d" + k) for k in ("w", "tmp", "xi")}
+    sim.init_laplacian_solver(bf)
+    g = O.Grid(n, nz, lx, lz, fdm)
+    X, Z = np.meshgrid(np.arange(n) * lx / n, np.arange(nz) * lz / (nz - 1 if fdm else nz), indexing="ij")
+    if fdm:
+        V["tmp"].load(workloads.conductive(n, nz, lx, lz, seed=2), is_physical=True)
+        V["w"].load(40.0 * np.sin(np.pi * X) * np.sin(np.pi * Z), is_physical=True)
+        step = equations.rayleigh_benard(sim, V["w"], D["w"], V["tmp"], D["tmp"], 1.0, 1e4)
+    else:
+        rng = np.random.default_rng(5)
+        V["w"].load(3.0 * np.sin(2 * np.pi * X / lx) * np.cos(2 * np.pi * Z / lz) + 0.1 * rng.standard_normal((n, nz)),
+                    is_physical=True)
+        V["tmp"].load(np.cos(2 * np.pi * X / lx) * np.sin(2 * np.pi * Z / lz) + 0.05 * rng.standard_normal((n, nz)),
+                      is_physical=True)
+        V["xi"].load(0.5 * np.sin(4 * np.pi * Z / lz) + 0.05 * rng.standard_normal((n, nz)), is_physical=True)
+        step = equations.double_diffusive_spectral(sim, V["w"], D["w"], V["tmp"], D["tmp"], V["xi"], D["xi"],
+                                                   7.0, 1.1, 1.0 / 3.0)
+    sim.config_cfl(V["ux"], V["uz"])
+    sim.config_scalar_trackers({
+        "kinetic_energy.npz": functools.partial(calc_kinetic_energy, V["ux"], V["uz"], torch, p),
+        "nusselt_number.npz": functools.partial(calc_nusselt_number, V["tmp"], V["uz"], torch, p),
+    })
+    return sim, step, V, D["w"], g
+
+
+def _host_loop_with_tmp(sim, step, V):
+    """host_loop, with the temperature's physical field refreshed at the start
+    of each iteration (the example's loop body does it through
+    tmp.vec_dot_nabla)."""
+    from melvin.utility import calc_velocity_from_vorticity
+
+    solver = sim.get_laplacian_solver()
+    n = 0
+    while sim.is_running():
+        calc_velocity_from_vorticity(V["w"], V["psi"], V["ux"], V["uz"], solver)
+        V["tmp"].to_physical()
+        step.step()
+        sim.end_loop()
+        n += 1
+    return n
+
+
+@pytest.mark.parametrize("fdm,precision,tol", [(False, "double", 1e-12), (True, "double", 1e-12),
+                                               (False, "split", 2e-6)])
+def test_step_flux_diagnostic_vs_oracle(cuda, fdm, precision, tol):
+    """diag[3] = mean(tmp * uz) of the start-of-step fields against the
+    oracle's physical temperature and velocity, within `tol` times
+    mean(|tmp * uz|) (the mean itself may cancel)."""
+    sim, step, V, dw, g = _ddc_sim(precision=precision, fdm=fdm)
+    w_s, t_s = V["w"].gets().cpu().numpy(), V["tmp"].gets().cpu().numpy()
+    vel = O.velocity_from_vorticity(g, O.PoissonSolver(g), w_s)
+    prod = O.to_physical(g, t_s) * vel["uz_p"]
+    want, scale = float(np.mean(prod)), float(np.mean(np.abs(prod)))
+    want_ke = O.kinetic_energy(g, vel["ux_p"], vel["uz_p"])
+    step.set_flux_field(V["tmp"])
+    d = step.step(diagnostics=True).cpu().numpy()
+    assert abs(d[3] - want) <= tol * scale, (d[3], want, scale)
+    assert abs(d[0] - want_ke) <= tol * abs(want_ke)
+    step.set_flux_field(None)
+    assert step.step(diagnostics=True)[3].item() == 0.0
+
+
+@pytest.mark.parametrize("fdm", [False, True])
+def test_device_run_nusselt_tracker(cuda, fdm):
+    from melvin.driver import DeviceRun
+
+    a = _ddc_sim(fdm=fdm)
+    b = _ddc_sim(fdm=fdm)
+    na = _host_loop_with_tmp(a[0], a[1], a[2])
+    nb = DeviceRun(b[0], b[1], horizon=9).run(chunk=16)
+    assert na == nb > 100
+    sa, sb = a[0], b[0]
+    assert sa._loop_counter == sb._loop_counter and sa._t == sb._t
+    assert sa._integrator._dt == sb._integrator._dt
+    for ta, tb in zip(sa._trackers, sb._trackers):
+        assert ta._times == tb._times and len(ta._times) > 30
+        np.testing.assert_allclose(np.array(tb._values, dtype=float), np.array(ta._values, dtype=float),
+                                   rtol=1e-12, atol=1e-14)
+    nu = np.array(sb._trackers[1]._values, dtype=float)
+    assert np.all(np.isfinite(nu)) and np.ptp(nu) > 0
+    for k in ("w", "tmp"):
+        assert torch.equal(a[2][k]._sdata, b[2][k]._sdata), k
+
+
+def test_device_run_rejects_unknown_tracker(cuda):
+    from melvin.driver import DeviceRun
+
+    sim, step, V, dw, g = _ddc_sim()
+    sim._trackers[0]._filename = "enstrophy.npz"
+    sim._tracker_fns[0] = lambda: 0.0
+    with pytest.raises(ValueError, match="only the kinetic energy and the Nusselt number"):
+        DeviceRun(sim, step)
