@@ -275,6 +275,60 @@ def cpu_step_sample(w0, n, steps):
     return n * n * steps / dt / 1e6, dt
 
 
+def _oracle_member(job):
+    """One independent simulation of the oracle (reference algorithm, NumPy,
+    one thread) on one host core, time-bounded: returns (grid points x
+    steps, seconds).  `kind` "kh": a Kelvin-Helmholtz ensemble member
+    (256^2, vorticity + passive scalar, nu = kappa = 1e-4, dt = 5e-4, AB2
+    semi-implicit); "ddc": a serving-pool member (double-diffusive convection
+    on the Dirichlet grid, Ra_T = 1e6, Pr = 7, Le = 100, R_rho = 2, explicit
+    AB2, dt = 0.1 dz^2 / Pr)."""
+    kind, n, seed, budget = job
+    import numpy as np
+
+    import oracle as O
+    from oracle import problems as P
+
+    if kind == "kh":
+        g = O.Grid(n, n, 2 * np.pi, 2 * np.pi)
+        delta = np.random.default_rng(seed).uniform(0.02, 0.1)
+        w, c = P.kh_ic(g, delta, seed=seed)
+        pr = P.Problem(g, P.kh_specs(1e-4, 1e-4), [O.to_spectral(g, w), O.to_spectral(g, c)], 5e-4)
+    else:
+        g = O.Grid(n, n + 1, 2.0, 1.0, True, 2)
+        t0, s0 = P.conductive_ic(g, seed=2 * seed), P.conductive_ic(g, seed=2 * seed + 1)
+        pr = P.Problem(g, P.ddc_dirichlet_specs(7.0, 1e6, 2.0, 100.0),
+                       [np.zeros(g.spectral_shape, complex), O.to_spectral(g, t0), O.to_spectral(g, s0)],
+                       0.1 * g.dz ** 2 / 7.0, "explicit", 2)
+    pr.step()  # warm
+    steps, t_start = 0, time.perf_counter()
+    while True:
+        pr.step()
+        steps += 1
+        el = time.perf_counter() - t_start
+        if el >= budget and steps >= 2:
+            return g.nx * g.nz * steps, el
+
+
+def cpu_pool_sample(kind, n, members, budget=6.0):
+    """The oracle on min(host cores, members) cores: that many independent
+    members at once in a spawn pool, each time-bounded to `budget` seconds.
+    Aggregate Mpts.steps/s = total grid points x steps / the slowest
+    member's time."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+
+    cores = max(1, min(os.cpu_count() or 1, members))
+    # a worker that dies raises BrokenProcessPool here instead of being respawned
+    with ProcessPoolExecutor(max_workers=cores, mp_context=mp.get_context("spawn")) as pool:
+        res = list(pool.map(_oracle_member, [(kind, n, seed, budget) for seed in range(cores)], timeout=20 * budget))
+    pts = sum(r[0] for r in res)
+    secs = max(r[1] for r in res)
+    return {"value": round(pts / secs / 1e6, 4), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{cores} independent members at once, one per host core, each about {budget:.0f} s of "
+                      f"NumPy oracle steps after a warm step ({kind}, {n}x{n + (1 if kind == 'ddc' else 0)})"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -554,7 +608,8 @@ def run_ensemble(args):
         "tiles": list(ens.plan.get_tiles(2)),
         "tuned": None if tuned is None else {"default_ms": round(tuned.default_ms_per_step, 4),
                                              "ms": round(tuned.ms_per_step, 4)},
-        "l2": "flushed between graph launches"}), flush=True)
+        "l2": "flushed between graph launches",
+        "cpu_baseline": None if args.no_cpu else cpu_pool_sample("kh", n, members)}), flush=True)
     return 0
 
 
@@ -658,17 +713,19 @@ def run_ddc_pool(args):
     print(json.dumps({"workload": "ddc-pool", "grid": f"{nx}x{nz}", "slots": slots, "precision": args.precision,
                       "steps": args.steps, "ms_per_step": round(secs / args.steps * 1e3, 4),
                       "value": round(slots * nx * nz * args.steps / secs / 1e6, 2), "unit": UNIT,
-                      "l2": "flushed between steps"}), flush=True)
+                      "l2": "flushed between steps",
+                      "cpu_baseline": None if args.no_cpu else cpu_pool_sample("ddc", nx, slots)}), flush=True)
     return 0
 
 
 def run_rbc(args):
     """Rayleigh-Benard convection, one simulation: 1024 x 513 Fourier-x /
     Dirichlet-z grid, lx = 2, lz = 1, Ra = 1e7, Pr = 1, 4th-order finite
-    differences in z, AB4/AM4 predictor-corrector, dt = 1e-6 (the reference's
-    examples/rayleigh_benard_convection.py); temperature the conductive
-    profile plus 1e-3 seeded noise, vorticity zero.  FP64 unless --precision
-    says otherwise."""
+    differences in z, AB4/AM4 predictor-corrector, dt = 1e-7 (at Ra = 1e7
+    the reference's dt = 1e-6 of examples/rayleigh_benard_convection.py
+    overflows within 500 steps); temperature the conductive profile plus
+    1e-3 seeded noise, vorticity zero.  FP64 unless --precision says
+    otherwise."""
     import torch
 
     import melvin
@@ -677,7 +734,7 @@ def run_rbc(args):
     device = torch.device("cuda", dist_env()[2])
     torch.cuda.set_device(device)
     nx, nz, prec = 1024, 513, args.precision
-    p = melvin.Parameters({"nx": nx, "nz": nz, "lx": 2.0, "lz": 1.0, "final_time": 1.0, "initial_dt": 1e-6,
+    p = melvin.Parameters({"nx": nx, "nz": nz, "lx": 2.0, "lz": 1.0, "final_time": 1.0, "initial_dt": 1e-7,
                            "discretisation": ["spectral", "fdm"], "integrator": "explicit", "integrator_order": 4,
                            "spatial_derivative_order": 4, "precision": prec, "device": str(device)})
     sim = melvin.Simulation(p, torch)
@@ -700,7 +757,7 @@ def run_rbc(args):
         ev.append((e0, e1))
     torch.cuda.synchronize()
     secs = sum(a.elapsed_time(b) for a, b in ev) * 1e-3
-    print(json.dumps({"workload": "rbc", "grid": f"{nx}x{nz}", "integrator": "AB4/AM4 predictor-corrector",
+    print(json.dumps({"workload": "rbc", "grid": f"{nx}x{nz}", "integrator": "AB4/AM4 predictor-corrector", "dt": 1e-7,
                       "precision": prec, "steps": args.steps, "ms_per_step": round(secs / args.steps * 1e3, 4),
                       "value": round(nx * nz * args.steps / secs / 1e6, 2), "unit": UNIT,
                       "l2": "flushed between steps"}), flush=True)
