@@ -278,11 +278,13 @@ def cpu_step_sample(w0, n, steps):
 def _oracle_member(job):
     """One independent simulation of the oracle (reference algorithm, NumPy,
     one thread) on one host core, time-bounded: returns (grid points x
-    steps, seconds).  `kind` "kh": a Kelvin-Helmholtz ensemble member
+    steps, seconds, grid).  `kind` "kh": a Kelvin-Helmholtz ensemble member
     (256^2, vorticity + passive scalar, nu = kappa = 1e-4, dt = 5e-4, AB2
     semi-implicit); "ddc": a serving-pool member (double-diffusive convection
     on the Dirichlet grid, Ra_T = 1e6, Pr = 7, Le = 100, R_rho = 2, explicit
-    AB2, dt = 0.1 dz^2 / Pr)."""
+    AB2, dt = 0.1 dz^2 / Pr); "rbc": Rayleigh-Benard convection on the
+    n x (n/2 + 1) Dirichlet grid (Ra = 1e7, Pr = 1, 4th-order differences,
+    AB4/AM4 predictor-corrector, dt = 1e-7)."""
     kind, n, seed, budget = job
     import numpy as np
 
@@ -294,6 +296,11 @@ def _oracle_member(job):
         delta = np.random.default_rng(seed).uniform(0.02, 0.1)
         w, c = P.kh_ic(g, delta, seed=seed)
         pr = P.Problem(g, P.kh_specs(1e-4, 1e-4), [O.to_spectral(g, w), O.to_spectral(g, c)], 5e-4)
+    elif kind == "rbc":
+        g = O.Grid(n, n // 2 + 1, 2.0, 1.0, True, 4)
+        pr = P.Problem(g, P.rbc_specs(1.0, 1e7),
+                       [np.zeros(g.spectral_shape, complex), O.to_spectral(g, P.conductive_ic(g, seed=seed))],
+                       1e-7, "pece", 4)
     else:
         g = O.Grid(n, n + 1, 2.0, 1.0, True, 2)
         t0, s0 = P.conductive_ic(g, seed=2 * seed), P.conductive_ic(g, seed=2 * seed + 1)
@@ -307,7 +314,7 @@ def _oracle_member(job):
         steps += 1
         el = time.perf_counter() - t_start
         if el >= budget and steps >= 2:
-            return g.nx * g.nz * steps, el
+            return g.nx * g.nz * steps, el, f"{g.nx}x{g.nz}"
 
 
 def cpu_pool_sample(kind, n, members, budget=6.0):
@@ -325,8 +332,10 @@ def cpu_pool_sample(kind, n, members, budget=6.0):
     pts = sum(r[0] for r in res)
     secs = max(r[1] for r in res)
     return {"value": round(pts / secs / 1e6, 4), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{cores} independent members at once, one per host core, each about {budget:.0f} s of "
-                      f"NumPy oracle steps after a warm step ({kind}, {n}x{n + (1 if kind == 'ddc' else 0)})"}
+            "sample": (f"{cores} independent members at once, one per host core, each about {budget:.0f} s of "
+                       f"NumPy oracle steps after a warm step ({kind}, {res[0][2]})") if cores > 1 else
+                      (f"one simulation on one host core, about {budget:.0f} s of NumPy oracle steps after a warm "
+                       f"step ({kind}, {res[0][2]}; the reference is single-threaded)")}
 
 
 def run_reference(args):
@@ -760,7 +769,8 @@ def run_rbc(args):
     print(json.dumps({"workload": "rbc", "grid": f"{nx}x{nz}", "integrator": "AB4/AM4 predictor-corrector", "dt": 1e-7,
                       "precision": prec, "steps": args.steps, "ms_per_step": round(secs / args.steps * 1e3, 4),
                       "value": round(nx * nz * args.steps / secs / 1e6, 2), "unit": UNIT,
-                      "l2": "flushed between steps"}), flush=True)
+                      "l2": "flushed between steps",
+                      "cpu_baseline": None if args.no_cpu else cpu_pool_sample("rbc", nx, 1)}), flush=True)
     return 0
 
 
