@@ -570,35 +570,37 @@ struct FdXfArgs {
   Gate gate;
 };
 
-__device__ __forceinline__ zd fd_ab(const zd* h, size_t slot, int order, int curr, zd f0, double dt) {
+// History values f_{-1}, f_{-2}, f_{-3} of one element (AB2 uses the
+// first) from the ring of `order` slots (melvin/TimeDerivative.py:4-65).
+__device__ __forceinline__ void fd_hist_load(const zd* h, size_t slot, int order, int curr, zd hp[3]) {
   if (order == 2) {
-    const zd f1 = h[(size_t)((curr + 1) & 1) * slot];
-    const double c = dt / 2;
-    return mk(c * (3 * f0.x - f1.x), c * (3 * f0.y - f1.y));
+    hp[0] = h[(size_t)((curr + 1) & 1) * slot];
+    return;
   }
-  const zd f1 = h[(size_t)((curr + 3) & 3) * slot];
-  const zd f2 = h[(size_t)((curr + 2) & 3) * slot];
-  const zd f3 = h[(size_t)((curr + 1) & 3) * slot];
-  const double c = dt / 24;
-  return mk(c * (((55 * f0.x - 59 * f1.x) + 37 * f2.x) - 9 * f3.x),
-            c * (((55 * f0.y - 59 * f1.y) + 37 * f2.y) - 9 * f3.y));
+  hp[0] = h[(size_t)((curr + 3) & 3) * slot];
+  hp[1] = h[(size_t)((curr + 2) & 3) * slot];
+  hp[2] = h[(size_t)((curr + 1) & 3) * slot];
 }
-
-__device__ __forceinline__ zd fd_am(const zd* h, size_t slot, int order, int curr, zd f0, double dt) {
+// Adams-Bashforth and Adams-Moulton increments (melvin/Integrator.py:5-33)
+// of the newest value f0 and the history values hp.
+__device__ __forceinline__ zd fd_ab(int order, zd f0, const zd hp[3], double dt) {
   if (order == 2) {
-    const zd f1 = h[(size_t)((curr + 1) & 1) * slot];
     const double c = dt / 2;
-    return mk(c * (f0.x + f1.x), c * (f0.y + f1.y));
+    return mk(c * (3 * f0.x - hp[0].x), c * (3 * f0.y - hp[0].y));
   }
-  const zd f1 = h[(size_t)((curr + 3) & 3) * slot];
-  const zd f2 = h[(size_t)((curr + 2) & 3) * slot];
-  const zd f3 = h[(size_t)((curr + 1) & 3) * slot];
   const double c = dt / 24;
-  return mk(c * (((9 * f0.x + 19 * f1.x) - 5 * f2.x) + f3.x), c * (((9 * f0.y + 19 * f1.y) - 5 * f2.y) + f3.y));
+  return mk(c * (((55 * f0.x - 59 * hp[0].x) + 37 * hp[1].x) - 9 * hp[2].x),
+            c * (((55 * f0.y - 59 * hp[0].y) + 37 * hp[1].y) - 9 * hp[2].y));
 }
-
-// Boundary rules of examples/rayleigh_benard_convection.py:112-142 for
-// point (n, z); `e` = 1 (order 2) or 2 (order 4) edge points.
+__device__ __forceinline__ zd fd_am(int order, zd f0, const zd hp[3], double dt) {
+  if (order == 2) {
+    const double c = dt / 2;
+    return mk(c * (f0.x + hp[0].x), c * (f0.y + hp[0].y));
+  }
+  const double c = dt / 24;
+  return mk(c * (((9 * f0.x + 19 * hp[0].x) - 5 * hp[1].x) + hp[2].x),
+            c * (((9 * f0.y + 19 * hp[0].y) - 5 * hp[1].y) + hp[2].y));
+}
 __device__ __forceinline__ zd fd_bc(zd v, int bc, int n, int z, int nz, int e) {
   const bool lower = z < e, upper = z >= nz - e;
   if (bc & MGB_BC_DIRICHLET_W) {
@@ -615,8 +617,17 @@ __device__ __forceinline__ zd fd_bc(zd v, int bc, int n, int z, int nz, int e) {
   return v;
 }
 
+// Two resident CTAs of the x-forward pass where shared memory allows (the
+// register budget then stays at 128: the update holds every load of an
+// element for all fields at once).
 template <typename T, int N, int F, int CP>
-__global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
+struct FdXfOcc {
+  static constexpr size_t smem = (size_t)F * sbuf_elems<T, CP>(N) * sizeof(cx<T>);
+  static constexpr int value = 233472 / (smem + 1024) >= 2 ? 2 : 1;
+};
+
+template <typename T, int N, int F, int CP>
+__global__ void __launch_bounds__(NT, (FdXfOcc<T, N, F, CP>::value)) k_fd_xfwd(const FdXfArgs a) {
   if (gate_closed(a.gate)) return;
   const double dt = a.gate.dt ? *a.gate.dt : a.dt;
   constexpr int C = 2 * CP;
@@ -668,41 +679,47 @@ __global__ void __launch_bounds__(NT) k_fd_xfwd(const FdXfArgs a) {
       a.out[idx] = mk(v.x * a.inv_nx, v.y * a.inv_nx);
       continue;
     }
-    zd qs[F];
+    // every load of the element, for all fields, before the first store (the
+    // compiler cannot reorder loads above stores through these pointers)
+    zd qs[F], hd[F], q0[F], hp[F][3];
+    const zd ps = psi ? psi[idx] : mk(0.0, 0.0);
 #pragma unroll
-    for (int f = 0; f < F; ++f) qs[f] = qs_[f][idx];
+    for (int f = 0; f < F; ++f) {
+      qs[f] = qs_[f][idx];
+      hd[f] = hf[f][(size_t)a.curr * hslot + idx];
+      q0[f] = qf[f][idx];
+      fd_hist_load(hf[f] + idx, hslot, a.order, a.curr, hp[f]);
+    }
 #pragma unroll
     for (int f = 0; f < F; ++f) {
       cx<T> A, B;
       get_pair<T, N, CP>(buf + f * sbuf_elems<T, CP>(N), j, n, A, B);
       const zd v = cvt<double>(part ? B : A);
       // f = -vec_dot_nabla + linear terms + diffusion (already in the slot)
-      zd* hs = hf[f] + (size_t)a.curr * hslot + idx;
-      const zd d = *hs;
+      const zd d = hd[f];
       zd fv = mk(d.x - v.x * a.inv_nx, d.y - v.y * a.inv_nx);
       const FdXfField& eq = a.eq[f];
       for (int t = 0; t < eq.nterms; ++t) {
         const int sidx = eq.tsrc[t];
-        zd s = sidx < 0 ? psi[idx] : qs[0];
+        zd sv = sidx < 0 ? ps : qs[0];
 #pragma unroll
         for (int q2 = 1; q2 < F; ++q2)
-          if (sidx == q2) s = qs[q2];
+          if (sidx == q2) sv = qs[q2];
         if (eq.top[t] == 1) {
           const double b = g.dfx * (double)n;
-          s = mk(-(b * s.y), b * s.x);
+          sv = mk(-(b * sv.y), b * sv.x);
         }
         const double cc = tco ? tco[f * 4 + t] : eq.tcoef[t];
-        fv = mk(fv.x + cc * s.x, fv.y + cc * s.y);
+        fv = mk(fv.x + cc * sv.x, fv.y + cc * sv.y);
       }
-      *hs = fv;
-      const zd q0 = qf[f][idx];
+      hf[f][(size_t)a.curr * hslot + idx] = fv;
       zd qn;
       if (a.mode == FD_CORRECT) {
-        const zd am = fd_am(hf[f] + idx, hslot, a.order, a.curr, fv, dt);
-        qn = mk(q0.x + am.x, q0.y + am.y);
+        const zd am = fd_am(a.order, fv, hp[f], dt);
+        qn = mk(q0[f].x + am.x, q0[f].y + am.y);
       } else {
-        const zd ab = fd_ab(hf[f] + idx, hslot, a.order, a.curr, fv, dt);
-        qn = mk(q0.x + ab.x, q0.y + ab.y);
+        const zd ab = fd_ab(a.order, fv, hp[f], dt);
+        qn = mk(q0[f].x + ab.x, q0[f].y + ab.y);
       }
       qn = fd_bc(qn, eq.bc, n, z, g.nz, e_bc);
       if (a.mode == FD_PREDICT)
