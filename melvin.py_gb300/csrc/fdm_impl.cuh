@@ -743,7 +743,7 @@ __global__ void __launch_bounds__(NT, (FdXfOcc<T, N, F, CP>::value)) k_fd_xfwd(c
 //    FP32 tiles of 2048 elements below length 512, FdTile's from 512 on;
 //  * the x-forward pass takes the widest tile that still gives 1.5 CTAs per
 //    SM (a single simulation on a short z axis narrows it; pools keep it).
-// Double-float keeps FdTile's count (compile time).
+// Double-float follows the FP32 rules.
 inline int fd_sm_count() {
   static const int n = [] {
     int dev = 0, v = 0;
@@ -756,9 +756,8 @@ inline int fd_sm_count() {
 template <typename T, int N>
 struct FdCps {
   static constexpr int c0 = FdTile<T, N>::CP;
-  static constexpr bool narrow = !std::is_same<T, df64>::value;
-  static constexpr int c1 = narrow && c0 > 1 ? c0 / 2 : c0;
-  static constexpr int c2 = narrow && c1 > 1 ? c1 / 2 : c1;
+  static constexpr int c1 = c0 > 1 ? c0 / 2 : c0;
+  static constexpr int c2 = c1 > 1 ? c1 / 2 : c1;
   static constexpr int kInvElems = std::is_same<T, double>::value ? 1024 : (N >= 512 ? 4096 : 2048);
   static int xinv() {
     for (int cp : {c0, c1}) if (cp * N <= kInvElems) return cp;
