@@ -260,24 +260,32 @@ __device__ __forceinline__ T fd_imag(const cx<T>* buf, int col, int i, int sdo, 
 }
 
 // Replace the imaginary parts of columns [0, NCOL) by their periodic
-// z-derivative (in place, staged through registers).
+// z-derivative (in place, staged through registers).  A column's writes
+// only conflict with that column's reads, so groups of G columns share one
+// barrier (G x elements per thread <= 16 staged values).
 template <typename T, int N, int CS, int NCOL>
 __device__ __forceinline__ void fd_imag_columns(cx<T>* buf, int sdo, T inv) {
   constexpr int EPT = (N + NT - 1) / NT;
+  constexpr int G0 = 16 / EPT < 1 ? 1 : 16 / EPT;
+  constexpr int G = G0 < NCOL ? G0 : NCOL;
 #pragma unroll 1
-  for (int col = 0; col < NCOL; ++col) {
-    T v[EPT];
+  for (int c0 = 0; c0 < NCOL; c0 += G) {
+    T v[G][EPT];
 #pragma unroll
-    for (int i = 0; i < EPT; ++i) {
-      const int z = threadIdx.x + i * NT;
-      if (z < N) v[i] = fd_imag<T, N, CS>(buf, col, z, sdo, inv);
-    }
+    for (int g = 0; g < G; ++g)
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        const int z = threadIdx.x + i * NT;
+        if (c0 + g < NCOL && z < N) v[g][i] = fd_imag<T, N, CS>(buf, c0 + g, z, sdo, inv);
+      }
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < EPT; ++i) {
-      const int z = threadIdx.x + i * NT;
-      if (z < N) buf[sx<T, CS>(z, col)].y = v[i];
-    }
+    for (int g = 0; g < G; ++g)
+#pragma unroll
+      for (int i = 0; i < EPT; ++i) {
+        const int z = threadIdx.x + i * NT;
+        if (c0 + g < NCOL && z < N) buf[sx<T, CS>(z, c0 + g)].y = v[g][i];
+      }
   }
   __syncthreads();
 }
