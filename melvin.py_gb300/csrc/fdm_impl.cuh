@@ -439,7 +439,15 @@ __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
   constexpr int SX = FD_TX + 2 * H, SZ = FD_TZ + 2 * H;
   __shared__ T s_ux[SX][FD_TZ];  // x halo
   __shared__ T s_uz[FD_TX][SZ];  // z halo
-  __shared__ T s_q[SX][SZ];
+  // FP64 and double-float stage the products ux*q and uz*q once per point (as
+  // the reference forms them before differentiating, melvin/Variable.py:125-127):
+  // a third fewer operations on the narrow FP64 pipe (1024x513 RBC step 0.500
+  // -> 0.467 ms).  FP32 multiplies inside the stencil from staged q: the extra
+  // shared-memory pass costs it 2%.  The products are the same rounded values
+  // either way.
+  constexpr bool kStage = !std::is_same<T, float>::value;
+  __shared__ T s_a[kStage ? SX : 1][kStage ? FD_TZ : 1];  // ux*q, x halo
+  __shared__ T s_b[kStage ? FD_TX : SX][SZ];               // uz*q (z halo), or q (both halos)
   const GridC& g = a.g;
   const int nx = g.nx, nz = g.nz, sdo = g.sdo, h = sdo / 2;
   const int x0 = blockIdx.y * FD_TX, z0 = blockIdx.x * FD_TZ;
@@ -471,16 +479,31 @@ __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
   }
   for (int f = 0; f < a.nf; ++f) {
     const T* q = (const T*)maddr(a.q[f], nullptr, blockIdx.z);
-    for (int e = threadIdx.x; e < SX * SZ; e += NT) {
-      const int i = e / SZ, k = e - i * SZ;
-      const int x = (x0 + i - H + nx) % nx, z = z0 + k - H;
-      s_q[i][k] = (z >= 0 && z < nz) ? q[(size_t)x * nz + z] : (T)0;
-    }
-    __syncthreads();
-    if (a.partial.base && f == a.flux_f) {
-      for (int e = threadIdx.x; e < FD_TX * FD_TZ; e += NT) {
-        const int i = e / FD_TZ, k = e - i * FD_TZ;
-        if (x0 + i < nx && z0 + k < nz) fl += (double)s_uz[i][k + H] * (double)s_q[i + H][k + H];
+    const bool flux = a.partial.base && f == a.flux_f;
+    if constexpr (kStage) {
+      for (int e = threadIdx.x; e < SX * SZ; e += NT) {
+        const int i = e / SZ, k = e - i * SZ;
+        const int x = (x0 + i - H + nx) % nx, z = z0 + k - H;
+        const T qv = (z >= 0 && z < nz) ? q[(size_t)x * nz + z] : (T)0;
+        const bool in_z = k >= H && k < H + FD_TZ, in_x = i >= H && i < H + FD_TX;
+        if (in_z) s_a[i][k - H] = s_ux[i][k - H] * qv;
+        if (in_x) s_b[i - H][k] = s_uz[i - H][k] * qv;
+        if (flux && in_x && in_z && x0 + i - H < nx && z < nz) fl += (double)s_uz[i - H][k] * (double)qv;
+      }
+      __syncthreads();
+    } else {
+      auto& s_q = s_b;
+      for (int e = threadIdx.x; e < SX * SZ; e += NT) {
+        const int i = e / SZ, k = e - i * SZ;
+        const int x = (x0 + i - H + nx) % nx, z = z0 + k - H;
+        s_q[i][k] = (z >= 0 && z < nz) ? q[(size_t)x * nz + z] : (T)0;
+      }
+      __syncthreads();
+      if (flux) {
+        for (int e = threadIdx.x; e < FD_TX * FD_TZ; e += NT) {
+          const int i = e / FD_TZ, k = e - i * FD_TZ;
+          if (x0 + i < nx && z0 + k < nz) fl += (double)s_uz[i][k + H] * (double)s_q[i + H][k + H];
+        }
       }
     }
     T* jo = (T*)maddr(a.jout[f], nullptr, blockIdx.z);
@@ -489,12 +512,18 @@ __global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
       const int x = x0 + i, z = z0 + k;
       if (x >= nx || z >= nz) continue;
       const int ii = i + H, kk = k + H;
-      const T jx = st1(s_ux[ii + 2][k] * s_q[ii + 2][kk], s_ux[ii + 1][k] * s_q[ii + 1][kk],
-                       s_ux[ii - 1][k] * s_q[ii - 1][kk], s_ux[ii - 2][k] * s_q[ii - 2][kk], sdo, fdx);
-      T jz = 0;
-      if (z >= h && z < nz - h)
-        jz = st1(s_uz[i][kk + 2] * s_q[ii][kk + 2], s_uz[i][kk + 1] * s_q[ii][kk + 1],
-                 s_uz[i][kk - 1] * s_q[ii][kk - 1], s_uz[i][kk - 2] * s_q[ii][kk - 2], sdo, fdz);
+      T jx, jz = 0;
+      if constexpr (kStage) {
+        jx = st1(s_a[ii + 2][k], s_a[ii + 1][k], s_a[ii - 1][k], s_a[ii - 2][k], sdo, fdx);
+        if (z >= h && z < nz - h) jz = st1(s_b[i][kk + 2], s_b[i][kk + 1], s_b[i][kk - 1], s_b[i][kk - 2], sdo, fdz);
+      } else {
+        const auto& s_q = s_b;
+        jx = st1(s_ux[ii + 2][k] * s_q[ii + 2][kk], s_ux[ii + 1][k] * s_q[ii + 1][kk],
+                 s_ux[ii - 1][k] * s_q[ii - 1][kk], s_ux[ii - 2][k] * s_q[ii - 2][kk], sdo, fdx);
+        if (z >= h && z < nz - h)
+          jz = st1(s_uz[i][kk + 2] * s_q[ii][kk + 2], s_uz[i][kk + 1] * s_q[ii][kk + 1],
+                   s_uz[i][kk - 1] * s_q[ii][kk - 1], s_uz[i][kk - 2] * s_q[ii][kk - 2], sdo, fdz);
+      }
       jo[(size_t)x * nz + z] = jx + jz;
     }
     __syncthreads();
