@@ -433,7 +433,7 @@ __device__ __forceinline__ T st1(T p2, T p1, T m1, T m2, int sdo, T inv) {
 // J_f = pddx(ux q_f) + pddz(uz q_f) on a 2D tile (x periodic, z Dirichlet:
 // the outer sdo/2 points of pddz stay 0) (melvin/Variable.py:125-127).
 template <typename T>
-__global__ void __launch_bounds__(NT) k_fd_phys(const FdPhysArgs a) {
+__global__ void __launch_bounds__(NT, (std::is_same<T, float>::value ? 8 : 1)) k_fd_phys(const FdPhysArgs a) {
   if (gate_closed(a.gate)) return;
   constexpr int H = 2;  // storage halo (covers order 4)
   constexpr int SX = FD_TX + 2 * H, SZ = FD_TZ + 2 * H;
