@@ -496,6 +496,14 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
     }
   }
   __syncthreads();
+  // Up to 512 points (64-register kernels) the diagnostics are folded here,
+  // so the accumulators hold no registers through the forward transform
+  // (the 256-point KH ensemble kernel: 420 -> 196 bytes of spills); longer
+  // transforms fold at the end (measured 7% faster at 2048 points).
+  constexpr bool kEarlyDiag = N <= 512;
+  if constexpr (kEarlyDiag) {
+    if (a.partial) block_diag(ke, mx, mz, fl, a.partial + (size_t)blockIdx.y * gridDim.x * kDiagW);
+  }
   fd_imag_columns<T, N, CSO, P * NOUT>(buf, g.sdo, (T)a.fdz);
   block_fft<T, N, P * NOUT, CSO, NT, -1, RM>(buf, (const cx<T>*)a.tw);
   for (int m = threadIdx.x; m < nm; m += NT) {
@@ -516,7 +524,9 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
       }
     }
   }
-  if (a.partial) block_diag(ke, mx, mz, fl, a.partial + (size_t)blockIdx.y * gridDim.x * kDiagW);
+  if constexpr (!kEarlyDiag) {
+    if (a.partial) block_diag(ke, mx, mz, fl, a.partial + (size_t)blockIdx.y * gridDim.x * kDiagW);
+  }
 }
 
 // ---------------------------------------------------------------------------
