@@ -76,7 +76,8 @@ struct XTile {
 // of advected fields) by an autotuner that times them on the caller's own
 // workload.  Variant 0 is the default.
 //   x passes (k_xinv, k_xf_step): columns per CTA C and maximum FFT radix
-//     v = 0: C = XTile::C, radix 8; v = 1: C/2; v = 2: 2C; v = 3: C, radix 16
+//     v = 0: C = XTile::C (halved for the FP64 forward pass, XfVar), radix 8;
+//     v = 1: C/2; v = 2: 2C; v = 3: C, radix 16
 //   z pass (k_zz_step): row pairs per CTA P and maximum FFT radix
 //     v = 0: P = 1, radix 8; v = 1: P = 2; v = 2: P = 4; v = 3: P = 1, radix 16
 // Variants with the same shape share one kernel; those whose shared memory
@@ -87,6 +88,19 @@ constexpr int kTileVariants = 4;
 template <typename T, int N, int V>
 struct XVar {
   static constexpr int C0 = XTile<T, N>::C;
+  static constexpr int Cr = V == 1 ? C0 / 2 : (V == 2 ? 2 * C0 : C0);
+  static constexpr int C = Cr < 1 ? 1 : (Cr > 64 ? 64 : Cr);
+  static constexpr int RM = V == 3 ? 16 : 8;
+};
+
+// The forward x pass takes the same variants around a base tile that FP64
+// halves: that pass is bound by the FP64 pipe, and at 2048 points the
+// halved tile gives 683 CTAs instead of 341 (a full wave plus a 37-CTA
+// tail at two resident CTAs per SM): 0.172 -> 0.150 ms per launch.
+template <typename T, int N, int V>
+struct XfVar {
+  static constexpr int B = XTile<T, N>::C;
+  static constexpr int C0 = std::is_same<T, double>::value ? (B > 1 ? B / 2 : 1) : B;
   static constexpr int Cr = V == 1 ? C0 / 2 : (V == 2 ? 2 * C0 : C0);
   static constexpr int C = Cr < 1 ? 1 : (Cr > 64 ? 64 : Cr);
   static constexpr int RM = V == 3 ? 16 : 8;
@@ -944,7 +958,7 @@ cudaError_t launch_zz_step(const ZzArgs& a, int nb, cudaStream_t s) {
 
 template <typename T, int N, int F, int V>
 cudaError_t launch_xf_step(const XfArgs& a, int nb, cudaStream_t s) {
-  constexpr int C = XVar<T, N, V>::C, RM = XVar<T, N, V>::RM;
+  constexpr int C = XfVar<T, N, V>::C, RM = XfVar<T, N, V>::RM;
   const size_t smem = (size_t)F * sbuf_elems<T, C>(N) * sizeof(cx<T>);
   cudaError_t e = prep_smem(k_xf_step<T, N, F, C, RM>, smem);
   if (e != cudaSuccess) return e;
@@ -1039,9 +1053,9 @@ void fill_zz(FsLaunchers& L, int prec) {
 
 template <typename T, int N, int F, int V>
 void fill_xf(FsLaunchers& L, int prec) {
-  constexpr int C = XVar<T, N, V>::C;
+  constexpr int C = XfVar<T, N, V>::C;
   constexpr size_t smem = (size_t)F * sbuf_elems<T, C>(N) * sizeof(cx<T>);
-  L.xf_shape[prec][F - 1][V] = TileShape{C, XVar<T, N, V>::RM, smem <= kMaxDynSmem ? smem : 0};
+  L.xf_shape[prec][F - 1][V] = TileShape{C, XfVar<T, N, V>::RM, smem <= kMaxDynSmem ? smem : 0};
   if constexpr (smem <= kMaxDynSmem) {
     L.xf_step[prec][F - 1][V] = launch_xf_step<T, N, F, V>;
   } else {
@@ -1068,7 +1082,7 @@ void clear_step_variant(FsLaunchers& L, int prec) {
     L.zz_step[prec][f][V] = nullptr;
     L.xf_step[prec][f][V] = nullptr;
     L.zz_shape[prec][f][V] = TileShape{ZVar<V>::P, ZVar<V>::RM, 0};
-    L.xf_shape[prec][f][V] = TileShape{XVar<T, N, V>::C, XVar<T, N, V>::RM, 0};
+    L.xf_shape[prec][f][V] = TileShape{XfVar<T, N, V>::C, XfVar<T, N, V>::RM, 0};
   }
 }
 
