@@ -94,13 +94,13 @@ struct XVar {
 };
 
 // The forward x pass takes the same variants around a base tile that FP64
-// halves: that pass is bound by the FP64 pipe, and at 2048 points the
-// halved tile gives 683 CTAs instead of 341 (a full wave plus a 37-CTA
-// tail at two resident CTAs per SM): 0.172 -> 0.150 ms per launch.
+// and double-float halve: at 2048 points the halved tile gives 683 CTAs
+// instead of 341 (a full wave plus a 37-CTA tail at two resident CTAs per
+// SM): FP64 0.172 -> 0.150 ms per launch.
 template <typename T, int N, int V>
 struct XfVar {
   static constexpr int B = XTile<T, N>::C;
-  static constexpr int C0 = std::is_same<T, double>::value ? (B > 1 ? B / 2 : 1) : B;
+  static constexpr int C0 = std::is_same<T, float>::value ? B : (B > 1 ? B / 2 : 1);
   static constexpr int Cr = V == 1 ? C0 / 2 : (V == 2 ? 2 * C0 : C0);
   static constexpr int C = Cr < 1 ? 1 : (Cr > 64 ? 64 : Cr);
   static constexpr int RM = V == 3 ? 16 : 8;
