@@ -166,8 +166,8 @@ int mgb_velocity_from_vorticity(const mgb_plan* plan, const void* w_spec, void* 
 
 /* mgb_vec_dot_nabla for callers that cannot allocate device memory: code
  * running under a framework that owns every device allocation and passes a
- * kernel only its operands and results, or a section (real-time loop,
- * stream capture) where allocation is not allowed.  Same inputs, outputs
+ * kernel only its operands and results, or a real-time loop where
+ * allocation is not allowed.  Same inputs, outputs
  * and results as mgb_vec_dot_nabla, but the transform scratch comes from a
  * fixed MGB_NOALLOC_SCRATCH_BYTES array in the library's device memory
  * (held by every GPU that loads the library until the process exits), so
@@ -175,7 +175,8 @@ int mgb_velocity_from_vorticity(const mgb_plan* plan, const void* w_spec, void* 
  * complex128 fully spectral, nx*nz doubles for FDM-z; e.g. 512x512 fits)
  * are rejected with MGB_ERR_UNSUPPORTED.  The first call on a device looks
  * up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  All calls on a
+ * current; make that first call before any stream capture.  The plan's
+ * device must be current (MGB_ERR_INVALID otherwise).  All calls on a
  * device share the array: calls that overlap on the GPU race and must be
  * serialised by the caller.  No counterpart in the reference. */
 int mgb_vec_dot_nabla_noalloc(const mgb_plan* plan, const void* q_spec, double* q_phys, const double* ux,
@@ -318,6 +319,14 @@ int mgb_step_kernel_count(const mgb_plan* plan, const mgb_equation* eq, int32_t*
 int mgb_step_events(const mgb_plan* plan, const mgb_equation* eq, void* const* q, void* const* hist,
                     int32_t curr, double dt, void* work, double* diag, void* stream,
                     void* const* events, int32_t nevents);
+
+/* Throughput probe of the FP64 FMA pipe (the denominator of the FP64-ALU
+ * roofline of the FP64 step): launches `blocks` CTAs whose threads run
+ * independent chains of `iters` FP64 FMAs each and writes to *flops
+ * (host) the FP64 flops the launch retires (an FMA counts two); the caller
+ * times the launch on `stream`.  `sink` (device, `blocks` doubles) is never
+ * written in practice.  No reference counterpart (instrumentation). */
+int mgb_fp64_fma_probe(double* sink, int32_t blocks, int32_t iters, double* flops, void* stream);
 
 /* ---- device-driven run: the Simulation loop without host synchronisation --
  * The reference keeps t, dt and the loop counter on the host and, in

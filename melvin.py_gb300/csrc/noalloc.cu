@@ -3,9 +3,9 @@
 // Some callers cannot allocate device memory at the point where they need
 // the nonlinear term: code that runs inside a framework which owns every
 // device allocation and hands a kernel only its operands and results, or a
-// real-time / stream-capture section where allocating is not allowed.  This
-// entry point gives them mgb_vec_dot_nabla with its transform scratch taken
-// from a fixed array in the library's own device memory, so the call itself
+// real-time section where allocating is not allowed.  This entry point
+// gives them mgb_vec_dot_nabla with its transform scratch taken from a
+// fixed array in the library's own device memory, so the call itself
 // allocates nothing.
 //
 // The array is a file-scope __device__ object of MGB_NOALLOC_SCRATCH_BYTES;
@@ -13,7 +13,8 @@
 // calls on a device share it, so calls that overlap on the GPU (different
 // streams, or host threads racing on one stream) race on the scratch and
 // must be serialised by the caller.  Each call writes every scratch element
-// it later reads, so nothing needs clearing between calls.
+// it later reads, so nothing needs clearing between calls.  The call must
+// run with the plan's device current: the scratch address is per device.
 #include <mutex>
 
 #include "internal.h"
@@ -56,6 +57,11 @@ extern "C" int mgb_vec_dot_nabla_noalloc(const mgb_plan* p, const void* q_spec, 
   if (!p) return fail(MGB_ERR_INVALID, "%s: null plan", __func__);
   if (!q_spec || !q_phys || !ux || !uz || !out_spec) return fail(MGB_ERR_INVALID, "%s: null array", __func__);
   if (int st = need_exp_ffts(p, __func__)) return st;
+  int dev = -1;
+  MGB_CUDA(cudaGetDevice(&dev));
+  if (dev != p->device)
+    return fail(MGB_ERR_INVALID, "%s: the plan belongs to device %d but device %d is current; make the plan's "
+                "device current first", __func__, p->device, dev);
   const GridC& g = p->g;
   // scratch: two x-pass intermediates (fully spectral) or one physical field (FDM z)
   const size_t need = g.fdm ? (size_t)g.nx * g.nz * sizeof(double) : 2 * inter_bytes(g, MGB_PREC_DOUBLE);

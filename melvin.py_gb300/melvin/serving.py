@@ -46,6 +46,7 @@ class Request:
     admitted: float = None
     finished: float = None
     result: np.ndarray = None  # final spectral states (3, rows, cols) when kept
+    max_batch: int = 0         # most requests advanced together with this one in one batched launch
 
 
 @dataclasses.dataclass
@@ -138,6 +139,7 @@ class _Pool:
             self.event.record(self.stream)
         for st in self.active.values():
             st[1] += k
+            st[0].max_batch = max(st[0].max_batch, len(self.active))
         return k
 
     def busy(self):

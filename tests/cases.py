@@ -54,3 +54,14 @@ BASIS_TAGS = ["basis65x64_10", "basis65x64_20", "basis64x65_01", "basis64x65_02"
 def basis_grid(tag):
     nx, nz = (int(v) for v in tag[len("basis"):].split("_")[0].split("x"))
     return O.Grid(nx, nz, 1.0, 2.0)
+
+# Integrator.set_dt golden cases: tag -> grid
+CFL_GRIDS = {
+    "cfl_fs32": O.Grid(32, 32, TWO_PI, TWO_PI),
+    "cfl_fd32x17": O.Grid(32, 17, 2.0, 1.0, True, 2),
+}
+CFL_E2E_GRIDS = {
+    "cfl_e2e_fs32": O.Grid(32, 32, TWO_PI, TWO_PI),
+    "cfl_e2e_fd32x17": O.Grid(32, 17, 2.0, 1.0, True, 2),
+}
+CFL_CUTOFF = 0.5  # Parameters.cfl_cutoff default (melvin/Parameters.py:14)

@@ -257,6 +257,129 @@ def dirichlet_body(kappas, terms, pece=False):
     return pece_body if pece else explicit
 
 
+# dt / CFL-limit ratios tried on every velocity set: no shrink, no shrink,
+# four shrinks, seven shrinks, breach (cfl_cutoff = 0.5; every ratio is at
+# least 1% away from a shrink-count boundary 0.5 / 0.9^k)
+CFL_RATIOS = (0.01, 0.3, 0.7, 0.95, 1.2)
+
+
+def set_dt_outcomes(sim, ux, uz, dts):
+    """Integrator.set_dt (melvin/Integrator.py:35-44) from each dt in `dts`:
+    the dt it leaves, or NaN where it raises "CFL condition breached"."""
+    out = []
+    for dt in dts:
+        sim._integrator.override_dt(float(dt))
+        try:
+            with np.errstate(all="ignore"):
+                sim._integrator.set_dt(ux, uz)
+            out.append(sim._integrator.get_dt())
+        except Exception as e:  # the reference raises a bare Exception
+            assert str(e) == "CFL condition breached", e
+            out.append(np.nan)
+    return np.array(out, dtype=np.float64)
+
+
+def cfl_limit(p, vx, vz):
+    with np.errstate(all="ignore"):
+        return min(p.dx / np.max(vx), p.dz / np.max(vz))
+
+
+def cfl_cases(rng):
+    """set_dt on seeded velocity sets: plain random; a signed maximum far
+    below the absolute one; all-negative ux; ux = 0; a NaN in ux (caught:
+    Python's min keeps a NaN first argument); a NaN in uz (missed: min drops
+    a NaN second argument).  dts are CFL_RATIOS times the set's own limit
+    (the random set's limit where that is not a positive number)."""
+    for tag, p in (("cfl_fs32", params(32, 32, 2 * np.pi, 2 * np.pi)),
+                   ("cfl_fd32x17", params(32, 17, 2.0, 1.0, fdm=True, integrator="explicit"))):
+        with redirect_stdout(io.StringIO()):
+            sim = Simulation(p, np)
+        bf = [EXP, FDM] if p.discretisation[1] == "fdm" else [EXP, EXP]
+        ux, uz = sim.make_variable("ux", bf), sim.make_variable("uz", bf)
+        a = rng.standard_normal((p.nx, p.nz))
+        b = rng.standard_normal((p.nx, p.nz))
+        nan_a, nan_b = a.copy(), b.copy()
+        nan_a[3, 5] = np.nan
+        nan_b[7, 2] = np.nan
+        sets = {
+            "random": (a, b),
+            "signed": (0.25 - 4.0 * np.abs(a), 0.05 * b),
+            "negative": (-0.1 - np.abs(a), b),
+            "zero_x": (np.zeros_like(a), b),
+            "nan_ux": (nan_a, b),
+            "nan_uz": (a, nan_b),
+        }
+        c0 = cfl_limit(p, a, b)
+        names = []
+        for name, (vx, vz) in sets.items():
+            c = cfl_limit(p, vx, vz)
+            dts = (c if c > 0 and np.isfinite(c) else c0) * np.array(CFL_RATIOS)
+            ux.setp(vx.copy())
+            uz.setp(vz.copy())
+            G[f"{tag}/{name}/ux"] = vx
+            G[f"{tag}/{name}/uz"] = vz
+            G[f"{tag}/{name}/max"] = np.array([np.max(vx), np.max(vz)])
+            G[f"{tag}/{name}/dts"] = dts
+            G[f"{tag}/{name}/dt_out"] = set_dt_outcomes(sim, ux, uz, dts)
+            names.append(name)
+        G[f"{tag}/sets"] = np.array(names)
+
+
+def cfl_e2e_cases():
+    """set_dt on the velocity the reference derives from a vorticity field
+    (calc_velocity_from_vorticity, melvin/utility.py:62-79), as the CFL
+    ticker sees it after the first loop iteration.  Fully spectral: a
+    narrow jet ux ~ -3 sech^2((z-pi)/0.3) (so max(ux) ~ 0.29 while
+    max|ux| ~ 2.7) plus a Taylor-Green cell; Dirichlet z: a convection roll
+    plus a jet-like vorticity."""
+    two_pi = 2 * np.pi
+    p = params(32, 32, two_pi, two_pi, dt=1e-3)
+    x = np.linspace(0, p.lx, p.nx, endpoint=False)
+    z = np.linspace(0, p.lz, p.nz, endpoint=False)
+    X, Z = np.meshgrid(x, z, indexing="ij")
+    d = 0.3
+    # u = -3 sech^2((z-pi)/d): w = du/dz = 6 sech^2 tanh / d (lap psi = -w, ux = -d psi/dz)
+    s2 = (1 / np.cosh((Z - np.pi) / d)) ** 2
+    w_fs = 6.0 * s2 * np.tanh((Z - np.pi) / d) / d + 0.4 * np.sin(X) * np.sin(Z)
+    pf = params(32, 17, 2.0, 1.0, fdm=True, integrator="explicit", dt=1e-5)
+    x = np.linspace(0, pf.lx, pf.nx, endpoint=False)
+    z = np.linspace(0, pf.lz, pf.nz, endpoint=False)
+    X, Z = np.meshgrid(x, z, indexing="ij")
+    w_fd = 50.0 * np.sin(np.pi * X) * np.sin(np.pi * Z) + 20.0 * np.sin(2 * np.pi * Z)
+    for tag, p, w0 in (("cfl_e2e_fs32", p, w_fs), ("cfl_e2e_fd32x17", pf, w_fd)):
+        with redirect_stdout(io.StringIO()):
+            sim = Simulation(p, np)
+        bf = [EXP, FDM] if p.discretisation[1] == "fdm" else [EXP, EXP]
+        V = {n: sim.make_variable(n, bf) for n in ("w", "psi", "ux", "uz")}
+        with redirect_stdout(io.StringIO()):
+            sim.init_laplacian_solver(bf)
+        V["w"].load(w0, is_physical=True)
+        calc_velocity_from_vorticity(V["w"], V["psi"], V["ux"], V["uz"], sim.get_laplacian_solver())
+        vx, vz = V["ux"].getp().copy(), V["uz"].getp().copy()
+        dts = cfl_limit(p, vx, vz) * np.array(CFL_RATIOS)
+        G[f"{tag}/init_w"] = w0
+        G[f"{tag}/ux"] = vx
+        G[f"{tag}/uz"] = vz
+        G[f"{tag}/max"] = np.array([np.max(vx), np.max(vz)])
+        G[f"{tag}/dts"] = dts
+        G[f"{tag}/dt_out"] = set_dt_outcomes(sim, V["ux"], V["uz"], dts)
+
+
+def load_resample_case(rng):
+    """Variable.load of a spectral array from a finer fully spectral grid
+    (melvin/Variable.py:67-85,142-151).  The reference resamples into a real
+    array, so only a real-valued input keeps its values; it is used here
+    where it works: a 64x64 spectrum (43 x 21) loaded on a 32x32 grid
+    (21 x 10)."""
+    with redirect_stdout(io.StringIO()):
+        sim = Simulation(params(32, 32, 2 * np.pi, 2 * np.pi), np)
+    v = sim.make_variable("v", [EXP, EXP])
+    fine = rng.standard_normal(params(64, 64, 2 * np.pi, 2 * np.pi).spectral_shape)
+    v.load(fine, is_physical=False)
+    G["load_resample/in_spec"] = fine
+    G["load_resample/out_spec"] = v.gets().copy()
+
+
 def main():
     rng = np.random.default_rng(12345)
     two_pi = 2 * np.pi
@@ -322,6 +445,13 @@ def main():
                          (65, 65, [COS, COS]), (65, 65, [SIN, SIN]), (65, 65, [SIN, COS]), (33, 65, [COS, SIN])]:
         tag = f"basis{nx}x{nz}_{int(bf[0])}{int(bf[1])}"
         basis_verbs(tag, params(nx, nz, 1.0, 2.0), bf, rb)
+
+    # ---- Integrator.set_dt ----
+    cfl_cases(np.random.default_rng(31))
+    cfl_e2e_cases()
+
+    # ---- host I/O ----
+    load_resample_case(np.random.default_rng(41))
 
     np.savez_compressed(OUT, **G)
     print(f"wrote {OUT}: {len(G)} arrays, {os.path.getsize(OUT) / 1024:.1f} KiB")

@@ -20,18 +20,40 @@ def _cfg(precision):
     return DDCConfig(Ra_T=1e5, precision=precision)
 
 
+class StepClock:
+    """A deterministic server clock: every reading advances it by `tick`
+    seconds, so arrivals are ordered by engine iterations, not by how fast
+    the GPU happens to run."""
+
+    def __init__(self, tick=1e-3):
+        self.t, self.tick = 0.0, tick
+
+    def __call__(self):
+        self.t += self.tick
+        return self.t
+
+
 def test_result_same_alone_and_in_mix(cuda):
+    """The target arrives a few engine iterations after five other requests,
+    three of them on its grid with 400 steps each (25 chunks of 16 steps, at
+    most one chunk per pool and iteration), so it is admitted while they run
+    and shares their batched launches.  Its result is bit-identical to the
+    same request served alone."""
     from melvin.serving import Request, Server
 
-    target = Request(rid=0, nx=64, nz=33, r_rho=2.0, nsteps=40, arrival=0.02, seed=7)
-    alone = Server(_cfg("split"), slots_per_block=4).run([target], keep_results=True)[0].result
-    mix = [Request(rid=i + 1, nx=nx, nz=nz, r_rho=1.5 + 0.5 * i, nsteps=30 + 10 * i, arrival=0.0, seed=100 + i)
+    target = Request(rid=0, nx=64, nz=33, r_rho=2.0, nsteps=40, arrival=0.005, seed=7)
+    alone = Server(_cfg("split"), slots_per_block=4).run([target], keep_results=True, time_fn=StepClock())[0]
+    assert alone.max_batch == 1
+    mix = [Request(rid=i + 1, nx=nx, nz=nz, r_rho=1.5 + 0.5 * i, nsteps=400, arrival=0.0, seed=100 + i)
            for i, (nx, nz) in enumerate([(64, 33), (32, 17), (64, 33), (128, 65), (64, 33)])]
-    target2 = Request(rid=0, nx=64, nz=33, r_rho=2.0, nsteps=40, arrival=0.02, seed=7)
-    out = Server(_cfg("split"), slots_per_block=4).run(mix + [target2], keep_results=True)
-    res = next(r for r in out if r.rid == 0).result
-    assert np.array_equal(res, alone)
+    target2 = Request(rid=0, nx=64, nz=33, r_rho=2.0, nsteps=40, arrival=0.005, seed=7)
+    out = Server(_cfg("split"), slots_per_block=4).run(mix + [target2], keep_results=True, time_fn=StepClock())
+    assert np.array_equal(target2.result, alone.result)
     assert all(r.finished is not None and r.finished >= r.arrival for r in out)
+    # it ran inside a batch: all three same-grid requests were in its launches
+    assert target2.max_batch == 4, target2.max_batch
+    same = [r for r in mix if (r.nx, r.nz) == (64, 33)]
+    assert all(r.admitted < target2.admitted < target2.finished < r.finished for r in same)
 
 
 def test_served_result_matches_oracle(cuda):

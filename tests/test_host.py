@@ -83,3 +83,37 @@ def test_term_validation():
         Term("psi", "d3dx3", 1.0)
     t = Term("psi", "ddx", -2)
     assert t.coef == -2.0
+
+
+def test_parameters_save_round_trip(tmp_path):
+    """Parameters.save (melvin/Parameters.py:94-96) writes the dictionary the
+    parameters were built from as JSON; building from the file again gives
+    the same derived values."""
+    import json
+
+    from melvin import Parameters
+
+    d = {"nx": 1024, "nz": 513, "lx": 2.0, "lz": 1.0, "final_time": 0.5, "Ra": 1e7, "Pr": 1.0,
+         "discretisation": ["spectral", "fdm"], "integrator": "explicit", "integrator_order": 4,
+         "spatial_derivative_order": 4, "initial_dt": 1e-7}
+    p = Parameters(d)
+    fname = tmp_path / "params.json"
+    p.save(str(fname))
+    with open(fname) as f:
+        back = json.load(f)
+    assert back == d
+    q = Parameters(back)
+    for k in ("spectral_shape", "physical_shape", "nn", "dx", "dz", "initial_dt", "dump_cadence",
+              "integrator", "integrator_order", "spatial_derivative_order", "discretisation"):
+        assert getattr(q, k) == getattr(p, k), k
+    assert q.Ra == 1e7 and q.Pr == 1.0
+    # the default file name is the reference's
+    import os
+
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        Parameters(d).save()
+        assert (tmp_path / "params.json").exists()
+    finally:
+        os.chdir(cwd)

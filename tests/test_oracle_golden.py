@@ -260,3 +260,45 @@ def test_kat_transform_sine_both():
     want[1, 1], want[-1, 1], want[3, 2], want[-3, 2] = 1.0, -1.0, 2.0, -2.0
     np.testing.assert_array_almost_equal(spec, want)
     np.testing.assert_array_almost_equal(M.to_physical_basis(g, spec, M.SIN, M.SIN), phys)
+
+
+def _oracle_set_dt(g, ux, uz, dt):
+    """The oracle's set_dt, NaN where it raises the CFL breach."""
+    from cases import CFL_CUTOFF
+
+    try:
+        with np.errstate(all="ignore"):
+            return O.cfl_dt(g, ux, uz, dt, CFL_CUTOFF)
+    except RuntimeError:
+        return np.nan
+
+
+@pytest.mark.parametrize("tag", ["cfl_fs32", "cfl_fd32x17"])
+def test_oracle_set_dt_matches_reference(golden, tag):
+    """Integrator.set_dt (melvin/Integrator.py:35-44) on every velocity set:
+    the dt left behind is bit-equal, breaches (signed maximum <= 0, a NaN in
+    ux) agree, and a NaN in uz alone is missed as the reference misses it."""
+    from cases import CFL_GRIDS
+
+    g = CFL_GRIDS[tag]
+    for s in golden[f"{tag}/sets"]:
+        ux, uz = golden[f"{tag}/{s}/ux"], golden[f"{tag}/{s}/uz"]
+        got = [_oracle_set_dt(g, ux, uz, dt) for dt in golden[f"{tag}/{s}/dts"]]
+        np.testing.assert_array_equal(got, golden[f"{tag}/{s}/dt_out"], err_msg=str(s))
+    assert np.isnan(golden[f"{tag}/nan_ux/dt_out"]).all()
+    assert not np.isnan(golden[f"{tag}/nan_uz/dt_out"][:4]).any()
+    assert np.isnan(golden[f"{tag}/negative/dt_out"]).all()
+
+
+@pytest.mark.parametrize("tag", ["cfl_e2e_fs32", "cfl_e2e_fd32x17"])
+def test_oracle_velocity_set_dt_matches_reference(golden, tag):
+    """set_dt on the velocity derived from a vorticity field: the oracle's
+    velocity equals the reference's and the dt outcomes are identical."""
+    from cases import CFL_E2E_GRIDS
+
+    g = CFL_E2E_GRIDS[tag]
+    vel = O.velocity_from_vorticity(g, O.PoissonSolver(g), O.to_spectral(g, golden[f"{tag}/init_w"]))
+    assert rel_l2(vel["ux_p"], golden[f"{tag}/ux"]) < TOL
+    assert rel_l2(vel["uz_p"], golden[f"{tag}/uz"]) < TOL
+    got = [_oracle_set_dt(g, vel["ux_p"], vel["uz_p"], dt) for dt in golden[f"{tag}/dts"]]
+    np.testing.assert_array_equal(got, golden[f"{tag}/dt_out"])

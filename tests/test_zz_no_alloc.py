@@ -46,14 +46,19 @@ def test_noalloc_matches_workspace_entry_point(cuda, nx, nz, fdm, order):
         assert rel(qp_new, qp_ref) < TOL, call
 
 
-def test_noalloc_rejects_grids_beyond_its_scratch(cuda):
+@pytest.mark.parametrize("nx,nz,fdm", [(1024, 1024, False), (2048, 2048, False), (1024, 513, True)])
+def test_noalloc_rejects_grids_beyond_its_scratch(cuda, nx, nz, fdm):
+    """Just past the 4 MiB scratch: 1024^2 fully spectral needs two
+    1024 x 341 complex128 intermediates (11 MB); 1024x513 with a Dirichlet z
+    axis needs one 1024 x 513 double field (4.2 MB).  The call returns
+    MGB_ERR_UNSUPPORTED with a message and launches nothing."""
     from melvin import _native as N
 
     lib = N.load_library()
-    plan = N.Plan(2048, 2048, 1.0, 1.0, False, 2, N.PREC_DOUBLE, cuda)
+    plan = N.Plan(nx, nz, 1.0, 1.0, fdm, 2, N.PREC_DOUBLE, cuda)
     rows, cols = plan.spectral_shape
     q = torch.zeros((rows, cols), dtype=torch.complex128, device=cuda)
-    p = torch.zeros((2048, 2048), dtype=torch.float64, device=cuda)
+    p = torch.zeros((nx, nz), dtype=torch.float64, device=cuda)
     st = lib.mgb_vec_dot_nabla_noalloc(plan.handle, N.ptr(q), N.ptr(p), N.ptr(p), N.ptr(p), N.ptr(q),
                                        N.stream_handle(cuda))
     assert st == N.MGB_ERR_UNSUPPORTED
