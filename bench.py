@@ -241,21 +241,54 @@ def load_traffic():
         return {}
 
 
-def roofline(model, kernel_ms, names, peak_gbs, peak_kind, traffic, key):
+def roofline(model, kernel_ms, names, peak_gbs, peak_kind, traffic, key, step_ms):
+    """The dominant kernel's algorithmic bytes over its event-timed launch
+    duration against the HBM peak, plus the same for the whole step
+    (step_achieved / step_frac: the step's algorithmic bytes over its
+    event-timed duration)."""
     avg = [statistics.mean(v) for v in kernel_ms]
     k = max(range(len(avg)), key=lambda i: avg[i])
     name = names[k]
     achieved = model[name]["bytes"] / (avg[k] * 1e-3) / 1e9
     tr = traffic.get(key, {}).get(name)
+    step_bytes = sum(m["bytes"] for m in model.values())
+    step_gbs = step_bytes / (step_ms * 1e-3) / 1e9
     return {
         "kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
         "frac": round(achieved / peak_gbs, 4), "peak_kind": peak_kind,
         "traffic": tr, "algorithmic_bytes": model[name]["bytes"], "avg_ms": round(avg[k], 4),
         "kernel_ms": {names[i]: round(avg[i], 4) for i in range(len(avg))},
+        "step_algorithmic_bytes": step_bytes, "step_ms": round(step_ms, 4),
+        "step_achieved": round(step_gbs, 1), "step_frac": round(step_gbs / peak_gbs, 4),
     }, k
 
 
-FP64_FMA_TFLOPS = 1.205  # measured on this machine's GB300 (FP64 FMA loop)
+def fp64_fma_peak(device, iters=1 << 14, reps=5):
+    """FP64 FMA throughput of this GPU in TFLOP/s (an FMA counts two flops),
+    measured live with the library's probe kernel (mgb_fp64_fma_probe: 4
+    CTAs of 256 threads per SM, 8 independent FMA chains per thread): the
+    fastest of `reps` event-timed launches after one warm launch."""
+    import ctypes as C
+
+    import torch
+
+    from melvin import _native as N
+
+    lib = N.load_library()
+    blocks = 4 * torch.cuda.get_device_properties(device).multi_processor_count
+    sink = torch.zeros(blocks, dtype=torch.float64, device=device)
+    flops = C.c_double()
+    best = None
+    for r in range(reps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        N.check(lib.mgb_fp64_fma_probe(N.ptr(sink), blocks, iters, C.byref(flops), N.stream_handle(device)))
+        e1.record()
+        torch.cuda.synchronize()
+        if r:
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+    return flops.value / (best * 1e-3) / 1e12
 
 
 def cpu_step_sample(w0, n, steps):
@@ -476,7 +509,8 @@ def run_native(args):
                                                           tune=not args.no_tune)
             secs = reduce_max(sum(per_step) * 1e-3, dist, device)
             model = kernel_model(n, prec == "split")
-            roof, kdom = roofline(model, per_kernel, names, peak, peak_kind, traffic, prec)
+            roof, kdom = roofline(model, per_kernel, names, peak, peak_kind, traffic, prec,
+                                  secs / args.steps * 1e3)
             results[key] = dict(secs=secs, per_kernel=per_kernel, roof=roof, kdom=kdom, model=model, run=run,
                                 tiles=_tiles_summary(run[3].plan, tuned),
                                 value=aggregate_throughput(n * n, args.steps, world, secs))
@@ -510,6 +544,20 @@ def run_native(args):
         acc["split"] = _accuracy(n, device, w0, "split")
         acc["dfloat"] = _accuracy(n, device, w0, "dfloat")
 
+    # the other benchmark configurations, one process and GPU (N = 1 only)
+    extra = {}
+    if rank == 0 and world == 1 and not args.headline_only:
+        del results["split"]["run"], results["dfloat"]["run"]
+        torch.cuda.empty_cache()
+        cpu_on = not args.no_cpu
+        with ClockSampler(local) as extra_clocks:
+            extra["rbc"] = rbc_result(device, "double", min(args.steps, 100), args.warmup, cpu_on, 4.0)
+            extra["kh_ensemble"] = kh_ensemble_result(device, "split", 256, max(args.steps, 64), args.warmup,
+                                                      None, not args.no_tune, cpu_on, 4.0)
+            torch.cuda.empty_cache()
+            extra["serving"] = serving_result(device, "split", 100, (50.0, 12.0), cpu_on, 4.0)
+        extra["clocks"] = extra_clocks.summary()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, csecs = cpu_step_sample(w0, n, 2)
@@ -522,9 +570,13 @@ def run_native(args):
         avg_k = [statistics.mean(v) for v in r64["per_kernel"]]
         kd = r64["kdom"]
         fl = r64["model"][names[kd]]["flops"] / (avg_k[kd] * 1e-3) / 1e12
-        fp64_roof = {"kernel": names[kd], "achieved_tflops": round(fl, 4), "peak_tflops": FP64_FMA_TFLOPS,
-                     "frac": round(fl / FP64_FMA_TFLOPS, 4),
-                     "note": "nominal 5 N log2 N flops per complex FFT; peak = measured FP64 FMA rate of this GB300"}
+        fma_peak = fp64_fma_peak(device)
+        step_fl = sum(m["flops"] for m in r64["model"].values()) / (r64["secs"] / args.steps) / 1e12
+        fp64_roof = {"kernel": names[kd], "achieved_tflops": round(fl, 4), "peak_tflops": round(fma_peak, 4),
+                     "frac": round(fl / fma_peak, 4), "step_achieved_tflops": round(step_fl, 4),
+                     "step_frac": round(step_fl / fma_peak, 4),
+                     "note": "nominal 5 N log2 N flops per complex FFT; peak = FP64 FMA rate measured in this run "
+                             "by mgb_fp64_fma_probe (FMA = 2 flops)"}
 
         def sub(key, dtype):
             r = results[key]
@@ -551,6 +603,11 @@ def run_native(args):
             "clocks": clocks.summary(),
             "wall_s_fp64_timed": round(wall, 3),
         }
+        if extra:
+            line["rbc"] = extra["rbc"]
+            line["kh_ensemble"] = extra["kh_ensemble"]
+            line["serving"] = extra["serving"]
+            line["configs_clocks"] = extra["clocks"]
         print(json.dumps(line), flush=True)
     barrier(dist)
     if dist is not None:
@@ -558,11 +615,14 @@ def run_native(args):
     return 0
 
 
-def run_ensemble(args):
-    """Kelvin-Helmholtz ensemble: 256 independent 256x256 runs (vorticity +
-    passive scalar, nu = kappa = 1e-4, dt = 5e-4, AB2 semi-implicit, split
-    precision), delta ~ U[0.02, 0.1] per member; all members advance in one
-    CUDA-graph launch of `graph_steps` steps."""
+def kh_ensemble_result(device, precision="split", members=256, steps=200, warmup=3, tiles=None, tune=True,
+                       cpu=True, cpu_budget=6.0):
+    """Kelvin-Helmholtz ensemble: `members` independent 256x256 runs
+    (vorticity + passive scalar, nu = kappa = 1e-4, dt = 5e-4, AB2
+    semi-implicit), delta ~ U[0.02, 0.1] per member; all members advance in
+    CUDA-graph replays of 8 batched steps, L2 flushed between replays.
+    Returns the result dict (value in Mpts.steps/s, the step's algorithmic
+    HBM bytes and their fraction of the peak, the CPU baseline)."""
     import numpy as np
     import torch
 
@@ -570,11 +630,9 @@ def run_ensemble(args):
     from melvin import workloads
     from melvin.ensemble import Ensemble, FieldSpec
 
-    device = torch.device("cuda", dist_env()[2])
-    torch.cuda.set_device(device)
-    n, members, graph_steps = 256, args.members, 8
+    n, graph_steps = 256, 8
     p = melvin.Parameters({"nx": n, "nz": n, "lx": 2 * np.pi, "lz": 2 * np.pi, "final_time": 1.0,
-                           "initial_dt": 5e-4, "precision": args.precision, "device": str(device)})
+                           "initial_dt": 5e-4, "precision": precision, "device": str(device)})
     ens = Ensemble(p, [FieldSpec(1e-4), FieldSpec(1e-4)], members)
     rng = np.random.default_rng(0)
     deltas = rng.uniform(0.02, 0.1, size=members)
@@ -582,13 +640,15 @@ def run_ensemble(args):
         w, c = workloads.kelvin_helmholtz(n, n, deltas[b], seed=b)
         ens.load_physical(b, [w, c])
     ens.step(5e-4)
-    tuned_box = []
-    _apply_tiles(args, ens.plan, 2, lambda: tuned_box.append(ens.autotune(5e-4)))
-    tuned = tuned_box[0] if tuned_box else None
+    tuned = None
+    if tiles:
+        ens.plan.set_tiles(2, [int(v) for v in tiles.split(",")])
+    elif tune:
+        tuned = ens.autotune(5e-4)
     replay = ens.graph(5e-4, graph_steps)
-    for _ in range(max(args.warmup, 1)):
+    for _ in range(max(warmup, 1)):
         replay()
-    nrep = max(1, args.steps // graph_steps)
+    nrep = max(1, steps // graph_steps)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
     ev = []
     for _ in range(nrep):
@@ -600,25 +660,38 @@ def run_ensemble(args):
         ev.append((e0, e1))
     torch.cuda.synchronize()
     secs = sum(a.elapsed_time(b) for a, b in ev) * 1e-3
-    steps = nrep * graph_steps
+    steps_run = nrep * graph_steps
     nn = (n - 1) // 3
     S, Pk = (2 * nn + 1) * nn, n * nn
-    wi = 8 if args.precision == "split" else 16
+    wi = 8 if precision == "split" else 16
     bytes_step = members * (16 * 10 * S + wi * 2 * 8 * Pk)
     peak, kind = load_peaks()
-    ms = secs / steps * 1e3
-    print(json.dumps({
-        "workload": "kh-ensemble", "metric": "Mpts·steps/s (ensemble)", "members": members, "grid": f"{n}x{n}",
-        "precision": args.precision, "steps": steps, "graph_steps": graph_steps,
-        "value": round(members * n * n * steps / secs / 1e6, 2), "unit": UNIT,
+    ms = secs / steps_run * 1e3
+    out = {
+        "members": members, "grid": f"{n}x{n}", "precision": precision, "steps": steps_run,
+        "graph_steps": graph_steps, "value": round(members * n * n * steps_run / secs / 1e6, 2), "unit": UNIT,
         "ms_per_ensemble_step": round(ms, 4),
-        "hbm": {"algorithmic_bytes_per_step": bytes_step, "achieved_gbs": round(bytes_step / (ms * 1e-3) / 1e9, 1),
-                "peak_gbs": peak, "frac": round(bytes_step / (ms * 1e-3) / 1e9 / peak, 4), "peak_kind": kind},
+        "roofline": {"bound": "hbm", "algorithmic_bytes_per_step": bytes_step,
+                     "step_achieved": round(bytes_step / (ms * 1e-3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+                     "step_frac": round(bytes_step / (ms * 1e-3) / 1e9 / peak, 4), "peak_kind": kind},
         "tiles": list(ens.plan.get_tiles(2)),
         "tuned": None if tuned is None else {"default_ms": round(tuned.default_ms_per_step, 4),
                                              "ms": round(tuned.ms_per_step, 4)},
         "l2": "flushed between graph launches",
-        "cpu_baseline": None if args.no_cpu else cpu_pool_sample("kh", n, members)}), flush=True)
+        "cpu_baseline": cpu_pool_sample("kh", n, members, cpu_budget) if cpu else None,
+    }
+    del ens, replay
+    return out
+
+
+def run_ensemble(args):
+    import torch
+
+    device = torch.device("cuda", dist_env()[2])
+    torch.cuda.set_device(device)
+    res = kh_ensemble_result(device, args.precision, args.members, args.steps, args.warmup, args.tiles,
+                             not args.no_tune, not args.no_cpu)
+    print(json.dumps({"workload": "kh-ensemble", "metric": "Mpts·steps/s (ensemble)", **res}), flush=True)
     return 0
 
 
@@ -727,37 +800,34 @@ def run_ddc_pool(args):
     return 0
 
 
-def run_rbc(args):
+def rbc_result(device, precision="double", steps=200, warmup=3, cpu=True, cpu_budget=6.0):
     """Rayleigh-Benard convection, one simulation: 1024 x 513 Fourier-x /
     Dirichlet-z grid, lx = 2, lz = 1, Ra = 1e7, Pr = 1, 4th-order finite
     differences in z, AB4/AM4 predictor-corrector, dt = 1e-7 (at Ra = 1e7
     the reference's dt = 1e-6 of examples/rayleigh_benard_convection.py
     overflows within 500 steps); temperature the conductive profile plus
-    1e-3 seeded noise, vorticity zero.  FP64 unless --precision says
-    otherwise."""
+    1e-3 seeded noise, vorticity zero.  L2 flushed between steps."""
     import torch
 
     import melvin
     from melvin import BasisFunctions as B, equations, workloads
 
-    device = torch.device("cuda", dist_env()[2])
-    torch.cuda.set_device(device)
-    nx, nz, prec = 1024, 513, args.precision
+    nx, nz = 1024, 513
     p = melvin.Parameters({"nx": nx, "nz": nz, "lx": 2.0, "lz": 1.0, "final_time": 1.0, "initial_dt": 1e-7,
                            "discretisation": ["spectral", "fdm"], "integrator": "explicit", "integrator_order": 4,
-                           "spatial_derivative_order": 4, "precision": prec, "device": str(device)})
+                           "spatial_derivative_order": 4, "precision": precision, "device": str(device)})
     sim = melvin.Simulation(p, torch)
     bf = [B.COMPLEX_EXP, B.FDM]
     w, dw = sim.make_variable("w", bf), sim.make_derivative("dw")
     t, dt_ = sim.make_variable("tmp", bf), sim.make_derivative("dtmp")
     t.load(workloads.conductive(nx, nz, 2.0, 1.0, seed=0), is_physical=True)
     step = equations.rayleigh_benard(sim, w, dw, t, dt_, 1.0, 1e7, integrator="pece")
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step.step()
     torch.cuda.synchronize()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
     ev = []
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.zero_()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
@@ -766,35 +836,101 @@ def run_rbc(args):
         ev.append((e0, e1))
     torch.cuda.synchronize()
     secs = sum(a.elapsed_time(b) for a, b in ev) * 1e-3
-    print(json.dumps({"workload": "rbc", "grid": f"{nx}x{nz}", "integrator": "AB4/AM4 predictor-corrector", "dt": 1e-7,
-                      "precision": prec, "steps": args.steps, "ms_per_step": round(secs / args.steps * 1e3, 4),
-                      "value": round(nx * nz * args.steps / secs / 1e6, 2), "unit": UNIT,
-                      "l2": "flushed between steps",
-                      "cpu_baseline": None if args.no_cpu else cpu_pool_sample("rbc", nx, 1)}), flush=True)
-    return 0
+    ms = secs / steps * 1e3
+    # algorithmic bytes of one explicit evaluation (F = 2, AB4): 17 S + 10 P,
+    # S = nn*nz complex128, P = nx*nz in the transform precision; the
+    # predictor-corrector evaluates twice
+    S = (nx - 1) // 3 * nz * 16
+    P = nx * nz * (4 if precision == "split" else 8)
+    bytes_step = 2 * (17 * S + 10 * P)
+    peak, kind = load_peaks()
+    return {"grid": f"{nx}x{nz}", "integrator": "AB4/AM4 predictor-corrector", "dt": 1e-7,
+            "precision": precision, "steps": steps, "ms_per_step": round(ms, 4),
+            "value": round(nx * nz * steps / secs / 1e6, 2), "unit": UNIT,
+            "roofline": {"bound": "hbm", "algorithmic_bytes_per_step": bytes_step,
+                         "step_achieved": round(bytes_step / (ms * 1e-3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+                         "step_frac": round(bytes_step / (ms * 1e-3) / 1e9 / peak, 4), "peak_kind": kind},
+            "l2": "flushed between steps",
+            "cpu_baseline": cpu_pool_sample("rbc", nx, 1, cpu_budget) if cpu else None}
 
 
-def run_serving(args):
-    """Poisson stream of double-diffusive convection solves (Fourier-x /
-    Dirichlet-z, grids 128x129..1024x1025, R_rho ~ U[1.5, 4], 200..2000
-    steps, Ra_T = 1e6, Pr = 7, Le = 100, split precision) through the
-    continuous-batching server."""
+def run_rbc(args):
     import torch
-
-    from melvin import serving
 
     device = torch.device("cuda", dist_env()[2])
     torch.cuda.set_device(device)
-    reqs = serving.poisson_requests(args.requests, rate=50.0, seed=0)
+    res = rbc_result(device, args.precision, args.steps, args.warmup, not args.no_cpu)
+    print(json.dumps({"workload": "rbc", **res}), flush=True)
+    return 0
+
+
+def cpu_serving_sample(reqs, budget=4.0):
+    """The oracle's per-core rate on each serving grid (double-diffusive
+    convection on the Dirichlet grid, one member per core, the grids run at
+    once in one spawn pool, each member time-bounded to `budget` seconds),
+    and what it implies for the request mix: with all C cores each solving
+    one request at a time, solves/s = C / mean over the requests of
+    (grid points x steps / that grid's per-core rate)."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+
+    grids = sorted({r.nx for r in reqs})
+    cores = max(1, os.cpu_count() or 1)
+    per = max(1, cores // len(grids))
+    jobs = [("ddc", n, seed, budget) for n in grids for seed in range(per)]
+    with ProcessPoolExecutor(max_workers=min(cores, len(jobs)), mp_context=mp.get_context("spawn")) as pool:
+        res = list(pool.map(_oracle_member, jobs, timeout=20 * budget))
+    rate = {}
+    for (kind, n, seed, _), (pts, secs, _) in zip(jobs, res):
+        rate.setdefault(n, []).append(pts / secs)
+    rate = {n: sum(v) / len(v) for n, v in rate.items()}  # grid points x steps per second per core
+    mean_s = sum(r.nx * r.nz * r.nsteps / rate[r.nx] for r in reqs) / len(reqs)
+    pts = sum(r.nx * r.nz * r.nsteps for r in reqs) / len(reqs)
+    return {"kind": "port", "cores": cores, "unit": "solves/s",
+            "value": round(cores / mean_s, 5),
+            "mpts_steps_per_s": round(cores * pts / mean_s / 1e6, 3),
+            "per_core_mpts_steps_per_s": {f"{n}x{n + 1}": round(v / 1e6, 3) for n, v in rate.items()},
+            "mean_solve_s_one_core": round(mean_s, 1),
+            "sample": (f"{per} oracle members per grid at once ({len(jobs)} processes), each about {budget:.0f} s "
+                       "of steps; solves/s implied for the same request mix with every core solving one "
+                       "request at a time (no queueing)")}
+
+
+def serving_result(device, precision="split", requests=100, rates=(50.0, 12.0), cpu=True, cpu_budget=4.0):
+    """Poisson streams of double-diffusive convection solves (Fourier-x /
+    Dirichlet-z, grids 128x129..1024x1025, R_rho ~ U[1.5, 4], 200..2000
+    steps, Ra_T = 1e6, Pr = 7, Le = 100) through the continuous-batching
+    server, one run per arrival rate: the configuration's 50/s, which is
+    above what the GPU finishes for this mix (the tail is the backlog), and
+    a lower rate the GPU keeps up with (the tail is the service time)."""
+    from melvin import serving
+
     warm = serving.poisson_requests(8, rate=1000.0, seed=99, steps=(5, 10))
-    serving.Server(serving.DDCConfig(precision=args.precision), device=str(device)).run(warm)
-    srv = serving.Server(serving.DDCConfig(precision=args.precision), device=str(device))
-    out = srv.run(reqs)
-    summ = serving.summarize(out)
-    print(json.dumps({"workload": "ddc-serving", "precision": args.precision, "arrival_rate_per_s": 50.0,
-                      **{k: round(v, 4) if isinstance(v, float) else v for k, v in summ.items()},
-                      "pools": {f"{k[0]}x{k[1]}": p.ens.nslots for k, p in srv.pools.items()},
-                      "admissions_deferred_for_memory": srv.refused}), flush=True)
+    serving.Server(serving.DDCConfig(precision=precision), device=str(device)).run(warm)
+    runs = []
+    for rate in rates:
+        reqs = serving.poisson_requests(requests, rate=rate, seed=0)
+        srv = serving.Server(serving.DDCConfig(precision=precision), device=str(device))
+        summ = serving.summarize(srv.run(reqs))
+        runs.append({"arrival_rate_per_s": rate,
+                     **{k: round(v, 4) if isinstance(v, float) else v for k, v in summ.items()},
+                     "pools": {f"{k[0]}x{k[1]}": p.ens.nslots for k, p in srv.pools.items()},
+                     "admissions_deferred_for_memory": srv.refused})
+        del srv
+    head = runs[0]
+    return {"precision": precision, "value": head["solves_per_s"], "unit": "solves/s",
+            "p50_s": head["p50_s"], "p99_s": head["p99_s"], "runs": runs,
+            "cpu_baseline": cpu_serving_sample(serving.poisson_requests(requests, rate=rates[0], seed=0),
+                                               cpu_budget) if cpu else None}
+
+
+def run_serving(args):
+    import torch
+
+    device = torch.device("cuda", dist_env()[2])
+    torch.cuda.set_device(device)
+    res = serving_result(device, args.precision, args.requests, cpu=not args.no_cpu)
+    print(json.dumps({"workload": "ddc-serving", **res}), flush=True)
     return 0
 
 
@@ -816,6 +952,8 @@ def main(argv=None):
                          "rbc: one Rayleigh-Benard simulation on a Dirichlet grid")
     ap.add_argument("--members", type=int, default=256, help="kh-ensemble members")
     ap.add_argument("--requests", type=int, default=200, help="serving requests")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="default workload: leave out the rbc, kh_ensemble and serving sub-objects")
     ap.add_argument("--precision", help="precision of the kh-ensemble / serving workloads (default split) "
                                         "and of rbc (default double)")
     args = ap.parse_args(argv)

@@ -196,6 +196,7 @@ SIGNATURES = {
     "mgb_tile_info_get": [_P, _I, _I, _I, C.POINTER(MgbTileInfo)],
     "mgb_plan_set_tiles": [_P, _I, C.POINTER(_I)],
     "mgb_plan_get_tiles": [_P, _I, C.POINTER(_I)],
+    "mgb_fp64_fma_probe": [_P, _I, _I, C.POINTER(_D), _P],
 }
 _RESTYPES = {"mgb_status_string": C.c_char_p, "mgb_last_error": C.c_char_p}
 
