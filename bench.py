@@ -457,8 +457,9 @@ def _tiles_summary(plan, tuned):
     tiles = plan.get_tiles(1)
     out = {}
     for fam, name in enumerate(FAMILIES):
-        _, shape, radix, _ = plan.tile_info(fam, 1, tiles[fam])
-        out[name] = {"variant": tiles[fam], "per_cta": shape, "radix": radix}
+        _, shape, radix, _, kind = plan.tile_info(fam, 1, tiles[fam])
+        out[name] = {"variant": tiles[fam], "per_cta": shape, "radix": radix,
+                     "kind": "registers" if kind else "shared-memory passes"}
     if tuned is not None:
         out["tuned"] = {"default_ms": round(tuned.default_ms_per_step, 4), "ms": round(tuned.ms_per_step, 4),
                         "trials": len(tuned.trials)}

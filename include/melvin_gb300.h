@@ -400,15 +400,19 @@ int mgb_run_step(const mgb_plan* plan, const mgb_equation* eq, void* const* q, v
                  void* stream);
 
 /* ---- tile variants of the fused step (fully spectral plans) -------------
- * Each of the three fused-step kernels comes in MGB_TILE_VARIANTS variants
- * that differ in the work given to one CTA and in the largest FFT radix:
+ * Each of the three fused-step kernels comes in up to MGB_TILE_VARIANTS
+ * variants that differ in the work given to one CTA, the largest FFT radix
+ * and the kind of transform:
  *   MGB_FAMILY_XINV, MGB_FAMILY_XFWD (x passes): columns per CTA;
  *   MGB_FAMILY_ZSTEP (z pass): pairs of grid rows per CTA.
- * Variant 0 is the default.  An autotuner times the variants on the
+ * Variants 0-3 keep the transform in shared memory (kind 0); z-pass variant
+ * 4 (FP32, lengths 128..4096) keeps every thread's points in registers and
+ * exchanges them through shared memory between passes (kind 1).  A fresh
+ * plan selects its fastest default per precision (mgb_plan_get_tiles).  An autotuner times the variants on the
  * caller's workload and sets the fastest per plan and field count.  The
  * reference leaves the equivalent choice to numpy.fft's internal plan
  * (melvin/SpectralTransformer.py:58,85,132,191). */
-#define MGB_TILE_VARIANTS 4
+#define MGB_TILE_VARIANTS 5
 typedef enum mgb_family {
   MGB_FAMILY_XINV = 0,   /* inverse x pass (velocity and fields to z-mode columns) */
   MGB_FAMILY_ZSTEP = 1,  /* z pass: to physical rows, products, z stencil, back */
@@ -419,7 +423,7 @@ typedef struct mgb_tile_info {
   int32_t available;    /* 1 when the variant exists for this plan (its shared memory fits) */
   int32_t shape;        /* columns per CTA (x passes) or row pairs per CTA (z pass) */
   int32_t radix;        /* largest FFT radix (8 or 16) */
-  int32_t reserved;
+  int32_t kind;         /* 0: shared-memory passes; 1: register-resident points */
   uint64_t smem_bytes;  /* dynamic shared memory per CTA */
 } mgb_tile_info;
 

@@ -278,6 +278,15 @@ int fs_plan_init(mgb_plan* p) {
   MGB_CUDA(cudaMalloc(&p->tab_f, tf.size() * sizeof(float)));
   MGB_CUDA(cudaMemcpy(p->tab_d, td.data(), td.size() * sizeof(double), cudaMemcpyHostToDevice));
   MGB_CUDA(cudaMemcpy(p->tab_f, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice));
+  // default z pass: the register-resident kernel where it exists (FP32;
+  // 2048^2 split step: z pass 55 -> 37 us), else variant 0
+  if (p->exp_ok && fs_launchers(g.nz) != nullptr && fs_launchers(g.nx) != nullptr) {
+    for (int F = 1; F <= 3; ++F) {
+      mgb_tile_info info;
+      fs_tile_info(p, MGB_FAMILY_ZSTEP, F, 4, &info);
+      if (info.available) p->tiles[F - 1][MGB_FAMILY_ZSTEP] = 4;
+    }
+  }
   return MGB_OK;
 }
 
@@ -404,10 +413,13 @@ int fs_tile_info(const mgb_plan* p, int family, int nfields, int v, mgb_tile_inf
     ts = &L->xf_shape[prec][nfields - 1][v];
     have = L->xf_step[prec][nfields - 1][v] != nullptr;
   }
+  // a z pass that covers several row pairs per CTA needs whole CTAs of rows
+  // (its diagnostics partials are folded per CTA)
+  if (family == MGB_FAMILY_ZSTEP && have && g.nx % (2 * ts->shape) != 0) have = false;
   out->available = have ? 1 : 0;
   out->shape = ts->shape;
   out->radix = ts->radix;
-  out->reserved = 0;
+  out->kind = ts->kind;
   out->smem_bytes = ts->smem;
   return MGB_OK;
 }

@@ -80,10 +80,13 @@ struct XTile {
 //     v = 1: C/2; v = 2: 2C; v = 3: C, radix 16
 //   z pass (k_zz_step): row pairs per CTA P and maximum FFT radix
 //     v = 0: P = 1, radix 8; v = 1: P = 2; v = 2: P = 4; v = 3: P = 1, radix 16
+//   z pass v = 4 (FP32, N = 128..4096): the register-resident kernel
+//     k_zz_reg (zreg.cuh), N/8 threads per row pair; x passes have no v = 4
 // Variants with the same shape share one kernel; those whose shared memory
 // does not fit are absent.  Columns and row pairs change only which CTA does
-// the work, so they give bit-identical results; the radix changes rounding.
-constexpr int kTileVariants = 4;
+// the work, so they give bit-identical results; the radix and the kind of
+// transform change rounding.
+constexpr int kTileVariants = 5;
 
 template <typename T, int N, int V>
 struct XVar {
@@ -1009,7 +1012,10 @@ cudaError_t launch_xf_out(const XfOutArgs& a, cudaStream_t s) {
 struct TileShape {
   int shape, radix;
   size_t smem;
+  int kind = 0;  // 0: shared-memory passes; 1: register-resident (k_zz_reg)
 };
+
+#include "zreg.cuh"
 
 // Table of launchers for one length N, filled by the per-N translation units.
 struct FsLaunchers {
@@ -1095,6 +1101,36 @@ void fill_or_clear(FsLaunchers& L, int prec) {
   }
 }
 
+// Variant 4: the register-resident z pass, FP32 only; no x-pass kernels.
+template <typename T, int N, int F>
+void fill_zz_reg(FsLaunchers& L, int prec) {
+  if constexpr (std::is_same<T, float>::value && ZrShape<N>::ok) {
+    constexpr size_t smem = ZrSmem<N, F>::bytes;
+    L.zz_shape[prec][F - 1][4] = TileShape{ZrShape<N>::PAIRS, 8, smem <= kMaxDynSmem ? smem : 0, 1};
+    if constexpr (smem <= kMaxDynSmem) {
+      L.zz_step[prec][F - 1][4] = launch_zz_reg<N, F>;
+    } else {
+      L.zz_step[prec][F - 1][4] = nullptr;
+    }
+  } else {
+    L.zz_step[prec][F - 1][4] = nullptr;
+    L.zz_shape[prec][F - 1][4] = TileShape{1, 8, 0, 1};
+  }
+}
+
+template <typename T, int N>
+void fill_variant4(FsLaunchers& L, int prec) {
+  L.xinv[prec][4] = nullptr;
+  L.xinv_shape[prec][4] = TileShape{XVar<T, N, 0>::C, 8, 0};
+  for (int f = 0; f < 3; ++f) {
+    L.xf_step[prec][f][4] = nullptr;
+    L.xf_shape[prec][f][4] = TileShape{XfVar<T, N, 0>::C, 8, 0};
+  }
+  fill_zz_reg<T, N, 1>(L, prec);
+  fill_zz_reg<T, N, 2>(L, prec);
+  fill_zz_reg<T, N, 3>(L, prec);
+}
+
 // The fused-step kernels of one precision, the tile variants in MASK (bit v
 // = variant v).  The double-float kernels are built in the default tile
 // only: they are several times larger to compile than the others.
@@ -1104,6 +1140,7 @@ void fill_step_kernels(FsLaunchers& L, int prec) {
   fill_or_clear<T, N, 1, (MASK & 2) != 0>(L, prec);
   fill_or_clear<T, N, 2, (MASK & 4) != 0>(L, prec);
   fill_or_clear<T, N, 3, (MASK & 8) != 0>(L, prec);
+  fill_variant4<T, N>(L, prec);
 }
 
 // The FP64 per-verb kernels.

@@ -94,7 +94,7 @@ class MgbTileInfo(C.Structure):
         ("available", C.c_int32),
         ("shape", C.c_int32),
         ("radix", C.c_int32),
-        ("reserved", C.c_int32),
+        ("kind", C.c_int32),
         ("smem_bytes", C.c_uint64),
     ]
 
@@ -138,7 +138,7 @@ RUN_TICK, RUN_CFL, RUN_TRACK = 1, 2, 4
 # kernel families of the fused step with tile variants (mgb_family)
 FAMILY_XINV, FAMILY_ZSTEP, FAMILY_XFWD = 0, 1, 2
 FAMILIES = ("xinv", "zstep", "xfwd")
-TILE_VARIANTS = 4
+TILE_VARIANTS = 5
 
 
 class MgbEquation(C.Structure):
@@ -295,10 +295,11 @@ class Plan:
     # ---- tile variants of the fused step (fully spectral plans) ----------
 
     def tile_info(self, family, nfields, variant):
-        """(available, shape, radix, smem_bytes) of one tile variant."""
+        """(available, shape, radix, smem_bytes, kind) of one tile variant
+        (kind 0: shared-memory passes, 1: register-resident points)."""
         info = MgbTileInfo()
         self.call("mgb_tile_info_get", int(family), int(nfields), int(variant), C.byref(info))
-        return bool(info.available), info.shape, info.radix, info.smem_bytes
+        return bool(info.available), info.shape, info.radix, info.smem_bytes, info.kind
 
     def get_tiles(self, nfields):
         t = (_I * 3)()

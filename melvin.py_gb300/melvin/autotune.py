@@ -54,14 +54,14 @@ class TuneResult:
 
 
 def variants(plan, nfields):
-    """Available variants of each family, one per distinct (shape, radix)."""
+    """Available variants of each family, one per distinct (shape, radix, kind)."""
     out = []
     for fam in range(len(N.FAMILIES)):
         seen, lst = set(), []
         for v in range(N.TILE_VARIANTS):
-            ok, shape, radix, _ = plan.tile_info(fam, nfields, v)
-            if ok and (shape, radix) not in seen:
-                seen.add((shape, radix))
+            ok, shape, radix, _, kind = plan.tile_info(fam, nfields, v)
+            if ok and (shape, radix, kind) not in seen:
+                seen.add((shape, radix, kind))
                 lst.append(v)
         out.append(lst)
     return out

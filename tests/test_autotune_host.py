@@ -44,19 +44,23 @@ def test_search_starts_from_current_selection():
 
 
 class FakePlan:
-    """tile_info of a plan whose variants 0 and 2 coincide and 3 does not fit."""
+    """tile_info of a plan whose variants 0 and 2 coincide, 3 does not fit,
+    and 4 has variant 0's shape and radix but the register-resident kind
+    (in the z family only)."""
 
     def tile_info(self, family, nfields, v):
-        shape = {0: 4, 1: 2, 2: 4, 3: 8}[v]
-        return (v != 3, shape, 8, 1024 * shape)
+        shape = {0: 4, 1: 2, 2: 4, 3: 8, 4: 4}[v]
+        kind = 1 if v == 4 else 0
+        return (v != 3 and (v != 4 or family == 1), shape, 8, 1024 * shape, kind)
 
 
 def test_variants_deduplicate_and_skip_unavailable():
     ch = autotune.variants(FakePlan(), 1)
-    assert ch == [[0, 1], [0, 1], [0, 1]]
+    assert ch == [[0, 1], [0, 1, 4], [0, 1]]
     d = autotune.describe(FakePlan(), 2)
     assert set(d) == {"xinv", "zstep", "xfwd"}
-    assert d["zstep"][3] == (3, False, 8, 8, 8192)
+    assert d["zstep"][3] == (3, False, 8, 8, 8192, 0)
+    assert d["zstep"][4] == (4, True, 4, 8, 4096, 1)
 
 
 def test_tune_rejects_other_objects():

@@ -40,7 +40,13 @@ def one_family_variants(plan, F):
 
 
 def radix_changed(plan, F, tiles):
-    return any(plan.tile_info(fam, F, v)[2] != plan.tile_info(fam, F, 0)[2] for fam, v in enumerate(tiles))
+    """The selection changes a family's FFT radix or kind of transform against
+    variant 0 (so the rounding changes, not only the CTA work split)."""
+    def key(fam, v):
+        info = plan.tile_info(fam, F, v)
+        return info[2], info[4]
+
+    return any(key(fam, v) != key(fam, 0) for fam, v in enumerate(tiles))
 
 
 @pytest.mark.parametrize("tag", ["tg32_o2_ab2", "tg32_o4_ab4", "kh64x32", "ddcs32"])
@@ -52,6 +58,7 @@ def test_every_variant_matches_reference_trajectory(cuda, golden, tag):
     plan = step.plan
     tried = one_family_variants(plan, F)
     assert len(tried) > 3
+    default = plan.get_tiles(F)
     try:
         for tiles in tried:
             plan.set_tiles(F, tiles)
@@ -68,7 +75,7 @@ def test_every_variant_matches_reference_trajectory(cuda, golden, tag):
                     assert err < TOL, (tiles, s, n, err)
             assert rel_l2(np.array(kes), golden[f"{tag}/ke"]) < TOL, tiles
     finally:
-        plan.set_tiles(F, (0, 0, 0))
+        plan.set_tiles(F, default)
 
 
 def _turbulence_states(n, precision, F, tiles_list, nsteps=2):
@@ -94,6 +101,7 @@ def _turbulence_states(n, precision, F, tiles_list, nsteps=2):
         ics = [w0, c0]
         fields = [(w, dw), (c, dc)]
     out = {}
+    default = step.plan.get_tiles(F)
     try:
         for tiles in tiles_list:
             step.plan.set_tiles(F, tiles)
@@ -105,7 +113,7 @@ def _turbulence_states(n, precision, F, tiles_list, nsteps=2):
                 step.step(2e-4)
             out[tiles] = [v.gets().clone() for v, _ in fields]
     finally:
-        step.plan.set_tiles(F, (0, 0, 0))
+        step.plan.set_tiles(F, default)
     return step.plan, g, ics, out
 
 
@@ -153,6 +161,7 @@ def test_tune_stepper_restores_state(cuda):
         step.step()
         ref.step()
     before = (w._sdata.clone(), dw._data.clone(), dw._curr_idx)
+    default = step.plan.get_tiles(1)
     try:
         res = step.autotune(force=True)
         assert torch.equal(w._sdata, before[0]) and torch.equal(dw._data, before[1]) and dw._curr_idx == before[2]
@@ -165,7 +174,7 @@ def test_tune_stepper_restores_state(cuda):
             ref.step()
         assert rel_l2(w.gets().cpu().numpy(), ref.q[0]) < TOL
     finally:
-        step.plan.set_tiles(1, (0, 0, 0))
+        step.plan.set_tiles(1, default)
 
 
 def test_tune_ensemble_members(cuda):
@@ -182,6 +191,7 @@ def test_tune_ensemble_members(cuda):
     members = torch.tensor([1, 3, 4], dtype=torch.int32, device=cuda)
     ens.step(dt, members)
     q0, h0, c0 = ens.q.clone(), ens.hist.clone(), ens.curr
+    default = ens.plan.get_tiles(2)
     for _ in range(4):
         ens.step(dt, members)
     a = ens.q.clone()
@@ -200,4 +210,4 @@ def test_tune_ensemble_members(cuda):
         for s in (0, 2, 5):
             assert torch.equal(ens.q[s], q0[s])
     finally:
-        ens.plan.set_tiles(2, (0, 0, 0))
+        ens.plan.set_tiles(2, default)
