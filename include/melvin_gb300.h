@@ -72,8 +72,12 @@ typedef enum mgb_deriv {
 /* Validate the grid, upload twiddle tables and (FDM-z) the tridiagonal
  * factors.  Replaces the set-up done by Simulation.__init__ and
  * Simulation.init_laplacian_solver (melvin/Simulation.py:19-50, 67-74,
- * melvin/LaplacianSolver.py:7-56).  Requires a power-of-two nx (and nz when
- * fully spectral), 16 <= n <= 4096; nz >= 5 for FDM-z. */
+ * melvin/LaplacianSolver.py:7-56).  Fully spectral: 9 <= nx, nz <= 4096;
+ * the fused kernels (mgb_vec_dot_nabla, mgb_velocity_from_vorticity,
+ * mgb_step and the batched step) need powers of two in [16, 4096], the
+ * transforms and pointwise verbs take any such length (transform lengths
+ * that are not powers of two run as Bluestein convolutions).  Fourier-x /
+ * FDM-z: a power-of-two nx in [16, 4096] and 5 <= nz <= 1800. */
 int mgb_plan_create(const mgb_grid* grid, mgb_plan** out);
 int mgb_plan_destroy(mgb_plan* plan);
 /* Spectral (rows, cols) and physical (nx, nz) shapes of the plan. */
@@ -96,9 +100,10 @@ int mgb_to_spectral(const mgb_plan* plan, const double* phys, void* spec, void* 
 /* ---- cosine and sine bases ---------------------------------------------
  * Basis functions per axis (melvin/BasisFunctions.py:5-9).  The reference
  * transforms a cosine or sine axis of n points as a mirrored periodic signal
- * of 2(n-1) points (melvin/SpectralTransformer.py:90-199); here that length
- * must be a power of two in [16, 4096], i.e. n = 2^k + 1, and a plan accepts
- * such an axis (complex-exponential verbs then return MGB_ERR_UNSUPPORTED).
+ * of 2(n-1) points (melvin/SpectralTransformer.py:90-199); here that length,
+ * like n on a complex-exponential axis, must lie in [16, 4096] (a power of
+ * two runs as a block FFT, any other length as a Bluestein convolution of
+ * power-of-two FFTs).
  * Unlike the reference, to_physical leaves its input unchanged (the
  * reference doubles the zeroth cosine mode of its input in place,
  * melvin/SpectralTransformer.py:122-125; the result equals the reference's

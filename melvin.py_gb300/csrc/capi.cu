@@ -97,6 +97,8 @@ static int upload_twiddles(int n, void** td, void** tf, void** tdf) {
 static void release(mgb_plan* p) {
   if (!p) return;
   for (auto& kv : p->tw_extra) cudaFree(kv.second);
+  for (auto& kv : p->blue)
+    for (void* q : kv.second) cudaFree(q);
   cudaFree(p->tw_x_d);
   cudaFree(p->tw_x_f);
   cudaFree(p->tw_x_df);
@@ -134,13 +136,14 @@ const void* mirror_twiddles(const mgb_plan* p, int L) {
 int need_exp_ffts(const mgb_plan* p, const char* fn) {
   if (p->exp_ok) return MGB_OK;
   return fail(MGB_ERR_UNSUPPORTED,
-              "%s: complex-exponential transforms need power-of-two nx and nz; this plan has an axis of 2^k+1 "
-              "points, which only the cosine and sine bases use", fn);
+              "%s: the fused complex-exponential kernels need power-of-two nx and nz; this plan has another axis "
+              "length, which the transforms and the pointwise verbs support", fn);
 }
 
-// An axis of n points that a cosine or sine basis turns into a power-of-two
-// transform of 2(n-1) points.
-static bool mirrored_len(int n) { return n > 2 && pow2_in_range(2 * (n - 1)); }
+// A fully spectral axis of n points: its transforms run for transform
+// lengths 16 <= L <= 4096, L = n (complex exponential) or 2(n-1) (cosine,
+// sine).
+static bool spectral_len(int n) { return n >= 9 && n <= 4096; }
 
 }  // namespace mgb
 
@@ -174,14 +177,12 @@ int mgb_plan_create(const mgb_grid* grid, mgb_plan** out) {
   *out = nullptr;
   const mgb_grid& G = *grid;
   const bool px = pow2_in_range(G.nx), pz = pow2_in_range(G.nz);
-  if (!px && (G.fdm_z || !mirrored_len(G.nx)))
+  if (!px && (G.fdm_z || !spectral_len(G.nx)))
     return fail(MGB_ERR_UNSUPPORTED,
-                "nx=%d: x transforms need a power of two in [16, 4096] (or 2^k+1 points with a cosine or sine "
-                "basis on a fully spectral grid)", G.nx);
-  if (!G.fdm_z && !pz && !mirrored_len(G.nz))
-    return fail(MGB_ERR_UNSUPPORTED,
-                "nz=%d: fully spectral z transforms need a power of two in [16, 4096] (or 2^k+1 points with a "
-                "cosine or sine basis)", G.nz);
+                "nx=%d: x transforms need 9..4096 points on a fully spectral grid, a power of two in [16, 4096] "
+                "with a Dirichlet z axis", G.nx);
+  if (!G.fdm_z && !pz && !spectral_len(G.nz))
+    return fail(MGB_ERR_UNSUPPORTED, "nz=%d: fully spectral z transforms need 9..4096 points", G.nz);
   if (G.fdm_z && (G.nz < 5 || G.nz > 1800))
     return fail(MGB_ERR_UNSUPPORTED, "nz=%d: FDM z axis needs 5 <= nz <= 1800", G.nz);
   if (G.sdo != 2 && G.sdo != 4)
@@ -256,9 +257,15 @@ int mgb_workspace_bytes(const mgb_plan* p, int32_t family, int32_t nfields, size
 
 int mgb_to_physical(const mgb_plan* p, const void* spec, double* phys, void* work, void* stream) {
   CHECK_PLAN(p);
-  if (int st = need_exp_ffts(p, __func__)) return st;
   CHECK_PTR(spec);
   CHECK_PTR(phys);
+  // an axis that is not a power of two: the basis path with both axes
+  // complex exponential (Bluestein transforms)
+  if (!p->exp_ok && !p->g.fdm) {
+    CHECK_PTR(work);
+    return mirror_to_physical(p, 0, 0, (const zd*)spec, phys, work, (cudaStream_t)stream);
+  }
+  if (int st = need_exp_ffts(p, __func__)) return st;
   if (p->g.fdm) return fd_to_physical(p, (const zd*)spec, phys, (cudaStream_t)stream);
   CHECK_PTR(work);
   return fs_to_physical(p, (const zd*)spec, phys, work, (cudaStream_t)stream);
@@ -266,9 +273,13 @@ int mgb_to_physical(const mgb_plan* p, const void* spec, double* phys, void* wor
 
 int mgb_to_spectral(const mgb_plan* p, const double* phys, void* spec, void* work, void* stream) {
   CHECK_PLAN(p);
-  if (int st = need_exp_ffts(p, __func__)) return st;
   CHECK_PTR(spec);
   CHECK_PTR(phys);
+  if (!p->exp_ok && !p->g.fdm) {
+    CHECK_PTR(work);
+    return mirror_to_spectral(p, 0, 0, phys, (zd*)spec, work, (cudaStream_t)stream);
+  }
+  if (int st = need_exp_ffts(p, __func__)) return st;
   if (p->g.fdm) return fd_to_spectral(p, phys, (zd*)spec, (cudaStream_t)stream);
   CHECK_PTR(work);
   return fs_to_spectral(p, phys, (zd*)spec, work, (cudaStream_t)stream);

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <map>
 #include <mutex>
 
@@ -43,13 +44,18 @@ struct mgb_plan {
   float* tab_f = nullptr;
   void* tab_df = nullptr;  // tux, tuz as double-float
   int device = 0;
-  // Both axes are power-of-two lengths, so complex-exponential transforms
-  // (every verb except the cosine/sine ones) can run.  An axis of 2^k + 1
-  // points is usable with cosine and sine bases only.
+  // Both axes are power-of-two lengths, so the complex-exponential kernels
+  // (the fused step, vec_dot_nabla, the velocity) can run.  A fully spectral
+  // plan with another axis length (9..4096 points) has the transforms of
+  // every basis (Bluestein for lengths that are not powers of two) and the
+  // pointwise spectral verbs.
   bool exp_ok = true;
   // Twiddle tables of other transform lengths (cosine/sine bases), by length
   // (guarded by mu).
   mutable std::map<int, void*> tw_extra;
+  // Bluestein tables of non-power-of-two transform lengths: chirp, forward
+  // and inverse kernel transforms (device), by length (guarded by mu).
+  mutable std::map<int, std::array<void*, 3>> blue;
   // Fused-step tile variants [nfields-1][mgb_family] (guarded by mu).
   int tiles[3][3] = {};
   mutable std::mutex mu;

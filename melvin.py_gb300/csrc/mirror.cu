@@ -12,41 +12,15 @@
 // x_factor * z_factor / (Lx * Lz): 1, 1/2 or -i/2 per axis, exact; to_spectral
 // multiplies by the rounded reciprocal of x_factor * z_factor.
 //
-// The kernels reuse the block FFT: a length-L transform for each axis, L a
-// power of two (so n = 2^k + 1 on a mirrored axis).  FP64 only (per-verb
-// transforms).
-#include "spectral2d_impl.cuh"
+// The kernels reuse the block FFT: a length-L transform for each axis when
+// L is a power of two (n = 2^k + 1 on a mirrored axis); other lengths in
+// [16, 4096] take the Bluestein twins of these kernels (bluestein.cu).
+// FP64 only (per-verb transforms).
+#include "mirror.cuh"
 
 namespace mgb {
 
 namespace {
-
-template <int L>
-struct MTile {
-  static constexpr int C0 = 4096 / L;
-  static constexpr int C = C0 < 1 ? 1 : (C0 > 64 ? 64 : C0);
-};
-
-struct MirrorArgs {
-  GridC g;
-  int nxp, nzp;          // physical extents
-  int lx, lz;            // transform lengths
-  int bx, bz;            // basis of each axis (0 exp, 1 cosine, 2 sine)
-  zd scale;              // to_physical: product of the per-axis factors; to_spectral: 1/(x_factor z_factor)
-  const zd* spec_in;
-  zd* spec_out;
-  const double* phys_in;
-  double* phys_out;
-  zd* inter;             // [nxp][nm]
-  const void* twx;
-  const void* twz;
-};
-
-__device__ __forceinline__ zd cmuld(zd a, zd b) { return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-
-// Position of kept spectral row r in a length-L x transform (rows 0..nn, then
-// the last nn bins), as _scale_2d places them (melvin/SpectralTransformer.py:21-24).
-__device__ __forceinline__ int mbin(int r, int nn, int L) { return r <= nn ? r : L - (2 * nn + 1 - r); }
 
 // to_physical, x pass: spectral column m -> length-Lx inverse transform ->
 // first nxp rows of the intermediate.
@@ -101,16 +75,6 @@ __global__ void __launch_bounds__(NT) k_mz_inv(const MirrorArgs a) {
     a.phys_out[(size_t)x0 * a.nzp + z] = w.x;
     if (two) a.phys_out[(size_t)(x0 + 1) * a.nzp + z] = w.y;
   }
-}
-
-// Mirror extension of a line of n points to L = 2(n-1) (sign s: +1 cosine,
-// -1 sine): j < n-1 -> v[j], j >= n-1 -> s * v[L-j]; an exp axis (L = n) is
-// the line itself.
-__device__ __forceinline__ int mirror_src(int j, int n, int L, int basis, double& sign) {
-  sign = 1.0;
-  if (basis == 0 || j < n - 1) return j;
-  sign = basis == 2 ? -1.0 : 1.0;
-  return L - j;
 }
 
 // to_spectral, z pass: two physical rows -> extension -> length-Lz r2c ->
@@ -230,6 +194,16 @@ int launched(cudaError_t e, const char* what) { return e == cudaSuccess ? MGB_OK
 int basis_length(int basis, int n) { return basis == 0 ? n : 2 * (n - 1); }
 
 static bool pow2_len(int n) { return n >= 16 && n <= 4096 && (n & (n - 1)) == 0; }
+static bool any_len(int n) { return n >= 16 && n <= 4096; }
+
+// One pass of a basis transform: the power-of-two kernel, or its Bluestein
+// twin for another length.
+static int mirror_pass(const mgb_plan* p, int L, int which, const MirrorArgs& a, cudaStream_t s, const char* what) {
+  if (pow2_len(L)) return launched(launch_mirror(L, which, a, s), what);
+  BlueTables b;
+  if (int st = bluestein_tables(p, L, b)) return st;
+  return launched(launch_bluestein(which, a, b, s), what);
+}
 
 static int mirror_args(const mgb_plan* p, int bx, int bz, MirrorArgs& a, const char* fn) {
   const GridC& g = p->g;
@@ -243,13 +217,14 @@ static int mirror_args(const mgb_plan* p, int bx, int bz, MirrorArgs& a, const c
   a.lz = basis_length(bz, g.nz);
   a.bx = bx;
   a.bz = bz;
-  if (!pow2_len(a.lx) || !pow2_len(a.lz))
+  if (!any_len(a.lx) || !any_len(a.lz))
     return fail(MGB_ERR_UNSUPPORTED,
                 "%s: transform lengths %d x %d (the basis needs 2(n-1) for cosine/sine and n for complex "
-                "exponentials to be a power of two in [16, 4096])", fn, a.lx, a.lz);
-  a.twx = mirror_twiddles(p, a.lx);
-  a.twz = mirror_twiddles(p, a.lz);
-  if (!a.twx || !a.twz) return fail(MGB_ERR_CUDA, "%s: twiddle tables for lengths %d, %d", fn, a.lx, a.lz);
+                "exponentials in [16, 4096])", fn, a.lx, a.lz);
+  a.twx = pow2_len(a.lx) ? mirror_twiddles(p, a.lx) : nullptr;
+  a.twz = pow2_len(a.lz) ? mirror_twiddles(p, a.lz) : nullptr;
+  if ((pow2_len(a.lx) && !a.twx) || (pow2_len(a.lz) && !a.twz))
+    return fail(MGB_ERR_CUDA, "%s: twiddle tables for lengths %d, %d", fn, a.lx, a.lz);
   return MGB_OK;
 }
 
@@ -263,9 +238,9 @@ int mirror_to_physical(const mgb_plan* p, int bx, int bz, const zd* spec, double
   a.spec_in = spec;
   a.phys_out = phys;
   a.inter = (zd*)work;
-  int st = launched(launch_mirror(a.lx, 0, a, s), "basis to_physical x pass");
+  int st = mirror_pass(p, a.lx, 0, a, s, "basis to_physical x pass");
   if (st) return st;
-  return launched(launch_mirror(a.lz, 1, a, s), "basis to_physical z pass");
+  return mirror_pass(p, a.lz, 1, a, s, "basis to_physical z pass");
 }
 
 int mirror_to_spectral(const mgb_plan* p, int bx, int bz, const double* phys, zd* spec, void* work, cudaStream_t s) {
@@ -279,9 +254,9 @@ int mirror_to_spectral(const mgb_plan* p, int bx, int bz, const double* phys, zd
   a.phys_in = phys;
   a.spec_out = spec;
   a.inter = (zd*)work;
-  int st = launched(launch_mirror(a.lz, 2, a, s), "basis to_spectral z pass");
+  int st = mirror_pass(p, a.lz, 2, a, s, "basis to_spectral z pass");
   if (st) return st;
-  return launched(launch_mirror(a.lx, 3, a, s), "basis to_spectral x pass");
+  return mirror_pass(p, a.lx, 3, a, s, "basis to_spectral x pass");
 }
 
 }  // namespace mgb

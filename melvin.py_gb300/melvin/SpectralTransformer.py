@@ -3,9 +3,10 @@
 Fully spectral grids use the 2D path (:90-199): 2/3 truncation to
 ``(2nn+1, nm)``, ``*nx*nz`` before the inverse and ``/(nx*nz)`` after the
 forward transform.  Fourier-x / FDM-z grids use the x-only path (:33-88).  Cosine and sine
-bases (:108-146, :169-196) use mirrored transforms of 2(n-1) points, which
-must be a power of two (n = 2^k + 1 on such an axis); unlike the reference,
-to_physical does not double the zeroth cosine mode of its input in place.
+bases (:108-146, :169-196) use mirrored transforms of 2(n-1) points; any
+transform length in [16, 4096] runs (powers of two as block FFTs, others as
+Bluestein convolutions).  Unlike the reference, to_physical does not double
+the zeroth cosine mode of its input in place.
 """
 
 import torch

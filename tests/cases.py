@@ -48,7 +48,9 @@ def params_dict(g, integrator="semi-implicit", order=2, dt=1e-3, precision="doub
 # Cosine / sine basis golden cases: tag -> grid (n = 2^k + 1 on a mirrored axis),
 # basis codes in the tag suffix (0 complex exponential, 1 cosine, 2 sine).
 BASIS_TAGS = ["basis65x64_10", "basis65x64_20", "basis64x65_01", "basis64x65_02", "basis65x65_11", "basis65x65_22",
-              "basis65x65_21", "basis33x65_12"]
+              "basis65x65_21", "basis33x65_12",
+              # transform lengths that are not powers of two: 78 x 48, 48 x 78, 64 x 88, 24 x 36, 258 x 198
+              "basis40x48_10", "basis48x40_02", "basis33x45_21", "basis24x36_00", "basis130x100_11"]
 
 
 def basis_grid(tag):

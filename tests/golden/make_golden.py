@@ -446,6 +446,13 @@ def main():
         tag = f"basis{nx}x{nz}_{int(bf[0])}{int(bf[1])}"
         basis_verbs(tag, params(nx, nz, 1.0, 2.0), bf, rb)
 
+    # ---- transform lengths that are not powers of two (2(n-1) or n) ----
+    rg = np.random.default_rng(2025)
+    for (nx, nz, bf) in [(40, 48, [COS, EXP]), (48, 40, [EXP, SIN]), (33, 45, [SIN, COS]), (24, 36, [EXP, EXP]),
+                         (130, 100, [COS, COS])]:
+        tag = f"basis{nx}x{nz}_{int(bf[0])}{int(bf[1])}"
+        basis_verbs(tag, params(nx, nz, 1.0, 2.0), bf, rg)
+
     # ---- Integrator.set_dt ----
     cfl_cases(np.random.default_rng(31))
     cfl_e2e_cases()

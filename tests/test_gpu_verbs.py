@@ -120,13 +120,31 @@ def test_round_trip_property_2048(cuda):
     assert rel_l2(host(back), host(s)) < TOL
 
 
-def test_unsupported_sizes_fail_loudly(cuda):
+def test_sizes_that_are_not_powers_of_two(cuda):
+    """A fully spectral 96 x 64 grid transforms like the oracle (the 96-point
+    axis as a Bluestein convolution) at 1e-12; the fused kernels refuse it
+    loudly, and so do an FDM-z grid with nx = 96 and an axis above 4096."""
     import melvin
+    from melvin import BasisFunctions as B
     from melvin._native import MelvinUnsupported
 
+    g = O.Grid(96, 64, 1.0, 1.0)
     p = melvin.Parameters({"nx": 96, "nz": 64, "lx": 1.0, "lz": 1.0, "final_time": 1.0})
+    sim = melvin.Simulation(p, torch)
+    rng = np.random.default_rng(96)
+    phys = rng.standard_normal((96, 64))
+    spec = sim._spectral_trans.to_spectral(torch.as_tensor(phys, device=cuda)).cpu().numpy()
+    assert rel_l2(spec, O.to_spectral(g, phys)) < TOL
+    back = sim._spectral_trans.to_physical(torch.as_tensor(spec, device=cuda)).cpu().numpy()
+    assert rel_l2(back, O.to_physical(g, spec)) < TOL
+    q = sim.make_variable("q", [B.COMPLEX_EXP, B.COMPLEX_EXP])
+    q.sets(spec)
     with pytest.raises(MelvinUnsupported):
-        melvin.Simulation(p, torch)
+        q.vec_dot_nabla(phys, phys)
+    for d in ({"nx": 96, "nz": 33, "discretisation": ["spectral", "fdm"]}, {"nx": 4100, "nz": 64}):
+        d.update(lx=1.0, lz=1.0, final_time=1.0)
+        with pytest.raises(MelvinUnsupported):
+            melvin.Simulation(melvin.Parameters(d), torch)
 
 
 @pytest.mark.parametrize("nx,nz", [(64, 18), (64, 19), (64, 35), (64, 66), (64, 130), (64, 258), (32, 513),
