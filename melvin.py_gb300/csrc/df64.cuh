@@ -13,6 +13,14 @@
 // computed in df64 is accurate to ~1e-14 relative L2 while running on the
 // FP32 pipes, which issue about 60x faster than FP64 on GB300.
 //
+// Addition leaves its result unnormalised: the exact two-sum of the high
+// words keeps the carry, and the low words are added into its error term
+// without the final fast two-sum (8 FP32 operations instead of 11).  The low
+// word may then reach a few ulps of the high one; two-sum is exact for any
+// operands and the product renormalises, so the pair keeps ~46 bits, the
+// conversion to double adds the halves exactly, and the error model above
+// is unchanged.
+//
 // The exponent range is FP32's: magnitudes below ~1e-30 lose low bits and
 // values below 1e-38 flush, which is far outside the range of the fields
 // transformed here.
@@ -47,7 +55,7 @@ __device__ __forceinline__ df64 df_fast_two_sum(float a, float b) {
 
 __device__ __forceinline__ df64 operator+(df64 a, df64 b) {
   const df64 s = df_two_sum(a.hi, b.hi);
-  return df_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+  return df64(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 
 __device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
