@@ -13,13 +13,15 @@
 // computed in df64 is accurate to ~1e-14 relative L2 while running on the
 // FP32 pipes, which issue about 60x faster than FP64 on GB300.
 //
-// Addition leaves its result unnormalised: the exact two-sum of the high
-// words keeps the carry, and the low words are added into its error term
-// without the final fast two-sum (8 FP32 operations instead of 11).  The low
-// word may then reach a few ulps of the high one; two-sum is exact for any
-// operands and the product renormalises, so the pair keeps ~46 bits, the
-// conversion to double adds the halves exactly, and the error model above
-// is unchanged.
+// Addition and multiplication leave their results unnormalised: the sum
+// keeps the exact two-sum of the high words and adds the low words into its
+// error term (8 FP32 operations instead of 11), the product keeps the exact
+// product of the high words and accumulates the cross terms into its error
+// term (4 instead of 7), without the final fast two-sum.  The low word may
+// then grow by a few ulps of the high one per operation; two-sum and the
+// FMA products are exact for any operands, the transforms renormalise every
+// value once per pass (pass_out in fft_block.cuh), so the pair keeps ~46
+// bits, and the conversion to double adds the halves exactly.
 //
 // The exponent range is FP32's: magnitudes below ~1e-30 lose low bits and
 // values below 1e-38 flush, which is far outside the range of the fields
@@ -46,11 +48,13 @@ __device__ __forceinline__ df64 df_two_sum(float a, float b) {
   return df64(s, e);
 }
 
-// Requires |a| >= |b| (or a == 0).
-__device__ __forceinline__ df64 df_fast_two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  const float e = __fsub_rn(b, __fsub_rn(s, a));
-  return df64(s, e);
+// Renormalise (hi, lo) to |lo| <= ulp(hi)/2: Dekker's fast two-sum, exact
+// when hi's exponent is at least lo's (the usual case: lo holds a few ulps
+// of hi); after a cancellation that left lo the larger, the error is
+// relative to that small value.
+__device__ __forceinline__ df64 df_renorm(df64 a) {
+  const float s = __fadd_rn(a.hi, a.lo);
+  return df64(s, __fsub_rn(a.lo, __fsub_rn(s, a.hi)));
 }
 
 __device__ __forceinline__ df64 operator+(df64 a, df64 b) {
@@ -67,7 +71,7 @@ __device__ __forceinline__ df64 operator*(df64 a, df64 b) {
   float e = __fmaf_rn(a.hi, b.hi, -p);
   e = __fmaf_rn(a.hi, b.lo, e);
   e = __fmaf_rn(a.lo, b.hi, e);
-  return df_fast_two_sum(p, e);
+  return df64(p, e);
 }
 
 }  // namespace mgb

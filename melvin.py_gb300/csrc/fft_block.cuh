@@ -134,6 +134,18 @@ struct PassRadix {
                                    : ((rem >= 8 && rem != 16) ? 8 : (rem >= 4 ? 4 : 2));
 };
 
+// A pass's outputs as stored for the next pass: double-float values are
+// renormalised (df_renorm), so the unnormalised low words that additions
+// and products leave behind grow over one pass only.
+template <typename T>
+__device__ __forceinline__ cx<T> pass_out(cx<T> v) {
+  return v;
+}
+template <>
+__device__ __forceinline__ cx<df64> pass_out(cx<df64> v) {
+  return mk(df_renorm(v.x), df_renorm(v.y));
+}
+
 template <typename T, int N, int C, int CS, int NT, int DIR, int R, int NS>
 __device__ __forceinline__ void stockham_pass(cx<T>* buf, const cx<T>* __restrict__ tw) {
   constexpr int NB = C * (N / R);
@@ -167,7 +179,7 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, const cx<T>* __restric
       const int k = i & (NS - 1);
       const int base = (i - k) * R + k;
 #pragma unroll
-      for (int r = 0; r < R; ++r) buf[sx<T, CS>(base + r * NS, c)] = v[t][r];
+      for (int r = 0; r < R; ++r) buf[sx<T, CS>(base + r * NS, c)] = pass_out(v[t][r]);
     }
   }
   __syncthreads();
