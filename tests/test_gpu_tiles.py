@@ -118,7 +118,8 @@ def _turbulence_states(n, precision, F, tiles_list, nsteps=2):
 
 
 @pytest.mark.parametrize("n,precision,F", [(512, "double", 1), (256, "double", 2), (512, "split", 1),
-                                           (256, "split", 2), (2048, "split", 1), (2048, "double", 1)])
+                                           (256, "split", 2), (2048, "split", 1), (2048, "double", 1),
+                                           (512, "dfloat", 1), (2048, "dfloat", 1)])
 def test_variants_agree(cuda, n, precision, F):
     import melvin
 
@@ -131,10 +132,10 @@ def test_variants_agree(cuda, n, precision, F):
         for a, b in zip(st, base):
             if radix_changed(plan, F, tiles):
                 err = (torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b)).item()
-                assert err < (1e-13 if precision == "double" else 1e-6), (tiles, err)
+                assert err < (1e-6 if precision == "split" else 1e-13), (tiles, err)
             else:
                 assert torch.equal(a, b), tiles
-    if precision == "double" and n <= 512:
+    if precision != "split" and n <= 512:
         specs = P.vorticity_specs(5e-5) if F == 1 else P.kh_specs(5e-5, 1e-4)
         ref = P.Problem(g, specs, [O.to_spectral(g, a) for a in ics], 2e-4)
         for _ in range(2):
