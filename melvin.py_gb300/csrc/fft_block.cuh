@@ -120,6 +120,113 @@ struct Dft<16, DIR, T> {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Butterflies with the twiddle products folded into FMAs (FP32 and FP64).
+// A DIT butterfly pair a + w v, a - w v computes the first as two chained
+// FMAs per component, t = fma(w.x, v.x, fma(-w.y, v.y, a.x)), and the second
+// as 2a - t (one FMA per component): 6 instructions where a separate
+// complex product and two additions take 8.  The sqrt(1/2) products of the
+// radix-8 odd terms fold into the final additions the same way.  Twiddled
+// radix-8: 72 FP instructions instead of 84; radix 4: 24 instead of 28.
+// Double-float keeps the plain form (its products are not fused).
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float fmx(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmx(double a, double b, double c) { return fma(a, b, c); }
+
+// v * w (DIR < 0) or v * conj(w) (DIR > 0)
+template <int DIR, typename T>
+__device__ __forceinline__ cx<T> tw_mul(cx<T> v, cx<T> w) {
+  return DIR < 0 ? mk(fmx(v.x, w.x, -(v.y * w.y)), fmx(v.x, w.y, v.y * w.x))
+                 : mk(fmx(v.x, w.x, v.y * w.y), fmx(v.y, w.x, -(v.x * w.y)));
+}
+// a + v * w (DIR < 0) or a + v * conj(w) (DIR > 0)
+template <int DIR, typename T>
+__device__ __forceinline__ cx<T> tw_fma(cx<T> a, cx<T> v, cx<T> w) {
+  return DIR < 0 ? mk(fmx(w.x, v.x, fmx(-w.y, v.y, a.x)), fmx(w.x, v.y, fmx(w.y, v.x, a.y)))
+                 : mk(fmx(w.x, v.x, fmx(w.y, v.y, a.x)), fmx(w.x, v.y, fmx(-w.y, v.x, a.y)));
+}
+// 2a - t
+template <typename T>
+__device__ __forceinline__ cx<T> twice_minus(cx<T> a, cx<T> t) {
+  return mk(fmx((T)2, a.x, -t.x), fmx((T)2, a.y, -t.y));
+}
+
+// Twiddled butterflies: a[r] *= w[r-1] (conjugated for DIR > 0) for r >= 1,
+// then the radix-R DFT, fused.  TW = false: no twiddles (w unused).
+template <int R, int DIR, typename T, bool TW>
+struct FDft;
+
+template <int DIR, typename T, bool TW>
+struct FDft<4, DIR, T, TW> {
+  static __device__ __forceinline__ void run(cx<T>* a, const cx<T>* w) {
+    if constexpr (!TW) {
+      dft4<4, DIR>(a[0], a[1], a[2], a[3]);
+    } else {
+      const cx<T> t0 = tw_fma<DIR>(a[0], a[2], w[1]);        // a0 + W2 a2
+      const cx<T> t1 = twice_minus(a[0], t0);                 // a0 - W2 a2
+      const cx<T> p = tw_mul<DIR>(a[1], w[0]);                // W1 a1
+      const cx<T> t2 = tw_fma<DIR>(p, a[3], w[2]);            // W1 a1 + W3 a3
+      const cx<T> t3 = mul_i<DIR>(twice_minus(p, t2));        // (W1 a1 - W3 a3) * (+-i)
+      a[0] = t0 + t2;
+      a[2] = t0 - t2;
+      a[1] = t1 + t3;
+      a[3] = t1 - t3;
+    }
+  }
+};
+
+template <int DIR, typename T, bool TW>
+struct FDft<8, DIR, T, TW> {
+  static __device__ __forceinline__ void run(cx<T>* a, const cx<T>* w) {
+    const T s = (T)0.70710678118654752440084436210484903928;
+    cx<T> t0, t1, t2, t3, u0, u1, u2, u3;
+    if constexpr (TW) {
+      // even inputs 0, 2, 4, 6 (twiddles w[1], w[3], w[5])
+      t0 = tw_fma<DIR>(a[0], a[4], w[3]);
+      t1 = twice_minus(a[0], t0);
+      const cx<T> p = tw_mul<DIR>(a[2], w[1]);
+      t2 = tw_fma<DIR>(p, a[6], w[5]);
+      t3 = mul_i<DIR>(twice_minus(p, t2));
+      // odd inputs 1, 3, 5, 7 (twiddles w[0], w[2], w[4], w[6])
+      const cx<T> p1 = tw_mul<DIR>(a[1], w[0]);
+      u0 = tw_fma<DIR>(p1, a[5], w[4]);
+      u1 = twice_minus(p1, u0);
+      const cx<T> p3 = tw_mul<DIR>(a[3], w[2]);
+      u2 = tw_fma<DIR>(p3, a[7], w[6]);
+      u3 = mul_i<DIR>(twice_minus(p3, u2));
+    } else {
+      t0 = a[0] + a[4];
+      t1 = a[0] - a[4];
+      t2 = a[2] + a[6];
+      t3 = mul_i<DIR>(a[2] - a[6]);
+      u0 = a[1] + a[5];
+      u1 = a[1] - a[5];
+      u2 = a[3] + a[7];
+      u3 = mul_i<DIR>(a[3] - a[7]);
+    }
+    const cx<T> e0 = t0 + t2, e2 = t0 - t2, e1 = t1 + t3, e3 = t1 - t3;
+    const cx<T> o0 = u0 + u2, o2 = mul_i<DIR>(u0 - u2), o1 = u1 + u3, o3 = u1 - u3;
+    // a[1] = e1 + s (1 + DIR i) o1, a[3] = e3 + s (-1 + DIR i) o3 (and minus for +4)
+    const T d1x = o1.x - (T)DIR * o1.y, d1y = o1.y + (T)DIR * o1.x;
+    const T d3x = -o3.x - (T)DIR * o3.y, d3y = -o3.y + (T)DIR * o3.x;
+    a[0] = e0 + o0;
+    a[4] = e0 - o0;
+    a[2] = e2 + o2;
+    a[6] = e2 - o2;
+    a[1] = mk(fmx(s, d1x, e1.x), fmx(s, d1y, e1.y));
+    a[5] = mk(fmx(-s, d1x, e1.x), fmx(-s, d1y, e1.y));
+    a[3] = mk(fmx(s, d3x, e3.x), fmx(s, d3y, e3.y));
+    a[7] = mk(fmx(-s, d3x, e3.x), fmx(-s, d3y, e3.y));
+  }
+};
+
+// Whether a radix and type take the fused butterflies.
+template <int R, typename T>
+struct Fused {
+  static constexpr bool value = (R == 8 || R == 4) && (std::is_same<T, float>::value || std::is_same<T, double>::value);
+};
+
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
 // Radix of the pass that starts with sub-transform length NS, at most RM
@@ -159,15 +266,25 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, const cx<T>* __restric
       const int c = b % C, i = b / C;
 #pragma unroll
       for (int r = 0; r < R; ++r) v[t][r] = buf[sx<T, CS>(i + r * (N / R), c)];
-      if (NS > 1) {
-        const int k = i & (NS - 1);
+      if constexpr (Fused<R, T>::value) {
+        cx<T> w[R - 1];
+        if constexpr (NS > 1) {
+          const int k = i & (NS - 1);
 #pragma unroll
-        for (int r = 1; r < R; ++r) {
-          const cx<T> w = tw[r * k * TWS];
-          v[t][r] = DIR < 0 ? cmul(v[t][r], w) : cmulc(v[t][r], w);
+          for (int r = 1; r < R; ++r) w[r - 1] = tw[r * k * TWS];
         }
+        FDft<R, DIR, T, (NS > 1)>::run(v[t], w);
+      } else {
+        if (NS > 1) {
+          const int k = i & (NS - 1);
+#pragma unroll
+          for (int r = 1; r < R; ++r) {
+            const cx<T> w = tw[r * k * TWS];
+            v[t][r] = DIR < 0 ? cmul(v[t][r], w) : cmulc(v[t][r], w);
+          }
+        }
+        Dft<R, DIR, T>::run(v[t]);
       }
-      Dft<R, DIR, T>::run(v[t]);
     }
   }
   __syncthreads();

@@ -95,11 +95,7 @@ __device__ __forceinline__ void zr_mid_pass(cx<float> (&v)[NCA][8], cx<float>* b
   for (int r = 0; r < 7; ++r) w[r] = wk[r];
   __syncthreads();  // every point of the buffer has been read
 #pragma unroll
-  for (int c = 0; c < NCOL; ++c) {
-#pragma unroll
-    for (int r = 1; r < 8; ++r) v[c][r] = zr_tw<DIR>(v[c][r], w[r - 1]);
-    Dft<8, DIR, float>::run(v[c]);
-  }
+  for (int c = 0; c < NCOL; ++c) FDft<8, DIR, float, true>::run(v[c], w);
   const int zb = zsw((t - k) * 8 + k);  // bit-disjoint from r * NS
 #pragma unroll
   for (int c = 0; c < NCOL; ++c)
@@ -138,9 +134,13 @@ __device__ __forceinline__ void zr_last_pass(cx<float> (&v)[NCA][8], const cx<fl
       cx<float> a[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) a[r] = v[c][j + r * G];
+      if constexpr (Fused<R, float>::value) {
+        FDft<R, DIR, float, true>::run(a, wp + 1);
+      } else {
 #pragma unroll
-      for (int r = 1; r < R; ++r) a[r] = zr_tw<DIR>(a[r], wp[r]);
-      Dft<R, DIR, float>::run(a);
+        for (int r = 1; r < R; ++r) a[r] = zr_tw<DIR>(a[r], wp[r]);
+        Dft<R, DIR, float>::run(a);
+      }
 #pragma unroll
       for (int r = 0; r < R; ++r) v[c][j + r * G] = a[r];
     }
@@ -158,7 +158,7 @@ __device__ __forceinline__ void zr_fft(cx<float> (&v)[NCA][8], cx<float>* buf, c
   if constexpr (SYNC_FIRST) __syncthreads();
 #pragma unroll
   for (int c = 0; c < NCOL; ++c) {
-    Dft<8, DIR, float>::run(v[c]);
+    FDft<8, DIR, float, false>::run(v[c], nullptr);
 #pragma unroll
     for (int r = 0; r < 8; ++r) buf[c * N + (z8 ^ r)] = v[c][r];
   }
