@@ -251,6 +251,10 @@ int fs_prepare(const mgb_plan* p, const mgb_equation* eq, double dt, void* work,
 
 int fs_plan_init(mgb_plan* p) {
   const GridC& g = p->g;
+  // The fused inverse transforms skip the inputs 3N/8 .. 5N/8 - 1 as removed
+  // modes: true of the 2/3 rule (nn = (nx - 1) / 3) at every power of two.
+  if ((fs_launchers(g.nx) && 8 * (g.nn + 1) > 3 * g.nx) || (fs_launchers(g.nz) && 8 * g.nm > 3 * g.nz))
+    return MGB_ERR_INVALID;
   const size_t S = (size_t)g.rows * g.cols;
   std::vector<double> td(3 * S);
   std::vector<float> tf(2 * S);

@@ -187,9 +187,14 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, sbuf_elems<T, C>(N) * sizeof(cx
   const int m0 = blockIdx.x * C;
   const T* tab = (const T*)(jb.kind == SRC_UX ? a.tux : a.tuz);
   const zd* src = jb.src + (size_t)batch_slot(a.b, blockIdx.z) * a.b.q_stride;
-  // zero the 2/3-rule gap rows nn+1 .. N-nn-1 (the kept rows are written below)
-  for (int e = threadIdx.x; e < (N - g.rows) * C; e += NT) {
-    const int x = g.nn + 1 + e / C, c = e % C;
+  // zero the 2/3-rule gap rows nn+1 .. N-nn-1 (the kept rows are written
+  // below), except 3N/8 .. 5N/8 - 1, which a pruned first pass does not read
+  // (nn < 3N/8 holds for every fully spectral plan)
+  constexpr bool zb = ZeroBand<N, RM, true>::value;
+  constexpr int skip = zb ? N / 4 : 0;
+  for (int e = threadIdx.x; e < (N - g.rows - skip) * C; e += NT) {
+    const int x0 = g.nn + 1 + e / C, c = e % C;
+    const int x = (zb && x0 >= 3 * N / 8) ? x0 + N / 4 : x0;
     buf[sx<T, C>(x, c)] = mk<T>(0, 0);
   }
   const int total = g.rows * C;
@@ -229,7 +234,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, sbuf_elems<T, C>(N) * sizeof(cx
     }
   }
   __syncthreads();
-  block_fft<T, N, C, C, NT, +1, RM>(buf, (const cx<T>*)a.tw);
+  block_fft<T, N, C, C, NT, +1, RM, true>(buf, (const cx<T>*)a.tw);
   cx<T>* out = (cx<T>*)((char*)jb.out + (size_t)blockIdx.z * a.b.inter_stride);
   for (int e = threadIdx.x; e < N * C; e += NT) {
     const int x = e / C, c = e - x * C, m = m0 + c;
@@ -451,9 +456,14 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
   const int xb = 2 * P * blockIdx.x;
   const int nm = g.cols, ld = a.ld;
   const size_t moff = (size_t)blockIdx.y * a.b.inter_stride;
-  // zero the modes nm .. N-nm of the input columns (the rest is written below)
-  for (int e = threadIdx.x; e < (N - 2 * nm + 1) * P * NIN; e += NT) {
-    const int z = nm + e / (P * NIN), c = e % (P * NIN);
+  // zero the modes nm .. N-nm of the input columns (the rest is written
+  // below), except 3N/8 .. 5N/8 - 1, which a pruned first pass does not read
+  // (nm <= 3N/8 holds for every fully spectral plan)
+  constexpr bool zb = ZeroBand<N, RM, true>::value;
+  constexpr int skip = zb ? N / 4 : 0;
+  for (int e = threadIdx.x; e < (N - 2 * nm + 1 - skip) * P * NIN; e += NT) {
+    const int z0 = nm + e / (P * NIN), c = e % (P * NIN);
+    const int z = (zb && z0 >= 3 * N / 8) ? z0 + N / 4 : z0;
     buf[sx<T, CS>(z, c)] = mk<T>(0, 0);
   }
   {
@@ -474,7 +484,7 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
     }
   }
   __syncthreads();
-  block_fft<T, N, P * NIN, CS, NT, +1, RM>(buf, (const cx<T>*)a.tw);
+  block_fft<T, N, P * NIN, CS, NT, +1, RM, true>(buf, (const cx<T>*)a.tw);
 
   double ke = 0.0, mx = -INFINITY, mz = -INFINITY, fl = 0.0;
   for (int z0 = 0; z0 < N; z0 += NT) {

@@ -150,15 +150,20 @@ __device__ __forceinline__ void zr_last_pass(cx<float> (&v)[NCA][8], const cx<fl
 // Whole transform of columns [0, NCOL): v holds point t + s*N/8 of every
 // column in register s on entry (the first pass's inputs) and on exit.
 // The buffer must be free to write on entry (SYNC_FIRST adds the barrier);
-// on exit every thread may still be reading it.
-template <int DIR, int N, int NCOL, int NCA, bool SYNC_FIRST>
+// on exit every thread may still be reading it.  ZB: registers 3 and 4 (the
+// points 3N/8 .. 5N/8 - 1) are zero and not read.
+template <int DIR, int N, int NCOL, int NCA, bool SYNC_FIRST, bool ZB = false>
 __device__ __forceinline__ void zr_fft(cx<float> (&v)[NCA][8], cx<float>* buf, const cx<float>* tab,
                                        const cx<float>* __restrict__ tw, int t) {
   const int zt = zsw(t), z8 = zsw(8 * t);  // bases of the reads and of the first-pass writes
   if constexpr (SYNC_FIRST) __syncthreads();
 #pragma unroll
   for (int c = 0; c < NCOL; ++c) {
-    FDft<8, DIR, float, false>::run(v[c], nullptr);
+    if constexpr (ZB) {
+      dft8_zero34<DIR>(v[c]);
+    } else {
+      FDft<8, DIR, float, false>::run(v[c], nullptr);
+    }
 #pragma unroll
     for (int r = 0; r < 8; ++r) buf[c * N + (z8 ^ r)] = v[c][r];
   }
@@ -258,6 +263,7 @@ __global__ void __launch_bounds__(ZrShape<N>::NTZ, (ZrOcc<N, F>::value)) k_zz_re
     }
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
+      if (s == 3 || s == 4) continue;  // removed modes (nm <= 3N/8): the pruned first pass skips them
       const int x = t + s * Q;
       const bool lo = x < nm, hi = x > N - nm;
       const int m = lo ? x : N - x;
@@ -272,7 +278,7 @@ __global__ void __launch_bounds__(ZrShape<N>::NTZ, (ZrOcc<N, F>::value)) k_zz_re
       }
     }
   }
-  zr_fft<+1, N, NIN, NC, false>(v, buf, tab, tw, t);
+  zr_fft<+1, N, NIN, NC, false, true>(v, buf, tab, tw, t);
 
   // products in registers: column f <- (ux0 q_f0, uz0 q_f0), column F+f <-
   // (ux1 q_f1, uz1 q_f1); diagnostics of the start-of-step velocity
