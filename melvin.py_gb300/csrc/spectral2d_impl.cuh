@@ -348,8 +348,9 @@ __device__ __forceinline__ void block_diag(double s, double mx, double mz, doubl
 // Fused z pass of the timestep: for P row pairs (rows x0 = 2*(P*blockIdx.x+p)
 // and x0+1, p < P),
 //   inverse c2r of ux, uz and the F advected fields,
-//   a_f = ux * q_f, b_f = uz * q_f, c_f = d/dz b_f (periodic stencil),
-//   forward r2c of a_f + i c_f, keep the nm leading modes.
+//   a_f = ux * q_f, b_f = uz * q_f, forward r2c of a_f + i b_f, keep the nm
+//   leading modes, C_f = d/dz B_f (the periodic stencil applied as its
+//   Fourier symbol: the same circulant operator, only rounding differs).
 // Pair p's inputs sit in columns p*NIN + i and its outputs in p*NOUT + j of
 // the CTA's buffer; a thread reads every input of a position z before it
 // writes that position's outputs.  Outputs may alias the inputs: a CTA reads
@@ -531,9 +532,15 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
   if constexpr (kEarlyDiag) {
     if (a.partial) block_diag(ke, mx, mz, fl, a.partial + (size_t)blockIdx.y * gridDim.x * kDiagW);
   }
-  fd_imag_columns<T, N, CSO, P * NOUT>(buf, g.sdo, (T)a.fdz);
   block_fft<T, N, P * NOUT, CSO, NT, -1, RM>(buf, (const cx<T>*)a.tw);
+  const cx<T>* twt = (const cx<T>*)a.tw;
+  const T fdz = (T)a.fdz;
   for (int m = threadIdx.x; m < nm; m += NT) {
+    // c = d/dz b by the periodic stencil is the circulant whose symbol at
+    // th = 2 pi m / N is i * sig, sig = 2 sin(th) fdz (order 2) or
+    // (4 sin(th) - sin(2 th) / 2) fdz (order 4), with tw[t] = exp(-2 pi i t / N)
+    const T s1 = -twt[m].y;
+    const T sig = g.sdo == 2 ? (T)2 * s1 * fdz : ((T)4 * s1 - (T)0.5 * (-twt[2 * m].y)) * fdz;
 #pragma unroll
     for (int p = 0; p < P; ++p) {
       const size_t r0 = (size_t)(xb + 2 * p) * ld, r1 = r0 + ld;
@@ -543,10 +550,10 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
         cx<T>* co = (cx<T>*)((char*)a.cout[f] + moff);
 #pragma unroll
         for (int rho = 0; rho < 2; ++rho) {
-          cx<T> A, Cc;
-          get_pair<T, N, CSO>(buf, p * NOUT + rho * F + f, m, A, Cc);
+          cx<T> A, B;
+          get_pair<T, N, CSO>(buf, p * NOUT + rho * F + f, m, A, B);
           ao[(rho ? r1 : r0) + m] = A;
-          co[(rho ? r1 : r0) + m] = Cc;
+          co[(rho ? r1 : r0) + m] = mk(-(sig * B.y), sig * B.x);
         }
       }
     }
