@@ -897,13 +897,15 @@ def cpu_serving_sample(reqs, budget=4.0):
                        "request at a time (no queueing)")}
 
 
-def serving_result(device, precision="split", requests=100, rates=(50.0, 12.0), cpu=True, cpu_budget=4.0):
+def serving_result(device, precision="split", requests=100, rates=(50.0, 12.0), cpu=True, cpu_budget=4.0,
+                   graphs=True):
     """Poisson streams of double-diffusive convection solves (Fourier-x /
     Dirichlet-z, grids 128x129..1024x1025, R_rho ~ U[1.5, 4], 200..2000
     steps, Ra_T = 1e6, Pr = 7, Le = 100) through the continuous-batching
     server, one run per arrival rate: the configuration's 50/s, which is
     above what the GPU finishes for this mix (the tail is the backlog), and
-    a lower rate the GPU keeps up with (the tail is the service time)."""
+    a lower rate the GPU keeps up with (the tail is the service time).
+    Chunks replay as captured CUDA graphs unless `graphs` is off."""
     from melvin import serving
 
     warm = serving.poisson_requests(8, rate=1000.0, seed=99, steps=(5, 10))
@@ -911,12 +913,12 @@ def serving_result(device, precision="split", requests=100, rates=(50.0, 12.0), 
     runs = []
     for rate in rates:
         reqs = serving.poisson_requests(requests, rate=rate, seed=0)
-        srv = serving.Server(serving.DDCConfig(precision=precision), device=str(device))
+        srv = serving.Server(serving.DDCConfig(precision=precision), device=str(device), graphs=graphs)
         summ = serving.summarize(srv.run(reqs))
         runs.append({"arrival_rate_per_s": rate,
                      **{k: round(v, 4) if isinstance(v, float) else v for k, v in summ.items()},
                      "pools": {f"{k[0]}x{k[1]}": p.ens.nslots for k, p in srv.pools.items()},
-                     "admissions_deferred_for_memory": srv.refused})
+                     "admissions_deferred_for_memory": srv.refused, "chunk_graphs": srv.graph_stats()})
         del srv
     head = runs[0]
     return {"precision": precision, "value": head["solves_per_s"], "unit": "solves/s",
@@ -930,7 +932,7 @@ def run_serving(args):
 
     device = torch.device("cuda", dist_env()[2])
     torch.cuda.set_device(device)
-    res = serving_result(device, args.precision, args.requests, cpu=not args.no_cpu)
+    res = serving_result(device, args.precision, args.requests, cpu=not args.no_cpu, graphs=not args.no_graphs)
     print(json.dumps({"workload": "ddc-serving", **res}), flush=True)
     return 0
 
@@ -943,6 +945,7 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
     ap.add_argument("--n", type=int, default=2048, help="grid points per side (default 2048)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-graphs", action="store_true", help="serving: launch every step from the host")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile variants (no autotuning)")
     ap.add_argument("--tiles", help="pin the tile variants x-inverse,z,x-forward (e.g. 0,1,1) instead of tuning")
     ap.add_argument("--only", choices=["fp64", "split", "dfloat"],

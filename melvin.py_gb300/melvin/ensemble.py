@@ -159,6 +159,40 @@ class Ensemble:
         replay.graph = g
         return replay
 
+    def chunk_graph(self, dt, nsteps, members, stream):
+        """Capture ``nsteps`` steps of ``members`` (a device int32 tensor whose
+        contents may change between replays; its address and length are
+        fixed at capture) from the current history slot into a CUDA graph on
+        ``stream``, without the device-wide synchronisation of
+        :meth:`graph`, so that other streams keep running.  Returns a callable
+        that replays the steps on the current stream and advances ``curr``;
+        it must be called with ``curr`` where it was at capture.  The capture
+        itself runs nothing."""
+        if not self._stepped:
+            raise RuntimeError("advance the ensemble once with step() before capturing")
+        self.prepare(dt)
+        curr0, end = self.curr, (self.curr + nsteps) % self.order
+        g = torch.cuda.CUDAGraph()
+        bt = self._batch(members)
+        with torch.cuda.stream(stream):
+            g.capture_begin(capture_error_mode="thread_local")
+            try:
+                for k in range(nsteps):
+                    N.check(self.plan.lib.mgb_batch_step(
+                        self.plan.handle, C.byref(self.eq), C.byref(bt), (curr0 + k) % self.order, float(dt),
+                        N.ptr(self.work), None, C.c_void_p(stream.cuda_stream)))
+            finally:
+                g.capture_end()
+
+        def replay():
+            if self.curr != curr0:
+                raise RuntimeError(f"chunk graph captured at history slot {curr0}, ensemble at {self.curr}")
+            g.replay()
+            self.curr = end
+
+        replay.graph = g
+        return replay
+
 
 class EnsembleGroup:
     """Ensembles of different grid sizes (or precisions) advanced together.

@@ -86,6 +86,10 @@ class _Pool:
         self.members = None
         self.stream = torch.cuda.Stream(device=server.device)
         self.event = None
+        self.use_graphs = server.use_graphs
+        self.mtab = None    # member table: the active slots, rewritten when they change
+        self.graphs = {}    # (members, steps, history slot) -> chunk-graph replay
+        self.captures = self.replays = 0
 
     @staticmethod
     def bytes_per_slot(server, nx, nz):
@@ -110,6 +114,8 @@ class _Pool:
         self.ens = new
         self.free = list(range(k, nslots))[::-1] + self.free
         self.members = None
+        self.mtab = None
+        self.graphs.clear()  # they hold the old ensemble's buffers
 
     def admit(self, req, cfg):
         slot = self.free.pop()
@@ -126,15 +132,42 @@ class _Pool:
 
     def launch(self, chunk):
         """Queue up to `chunk` steps of every active slot on the pool's stream
-        (no member overshoots its step count); returns the steps queued."""
+        (no member overshoots its step count); returns the steps queued.
+
+        With graphs on, the chunk is replayed as at most five CUDA graphs of
+        16, 8, 4, 2 and 1 steps, each captured once per (member count, step
+        count, history slot) over the pool's member table, whose contents
+        change with admissions and retirements while its address stays."""
         if not self.active:
             return 0
+        slots = sorted(self.active)
         if self.members is None:
-            self.members = torch.tensor(sorted(self.active), dtype=torch.int32, device=self.ens.device)
+            if not self.use_graphs:
+                self.members = torch.tensor(slots, dtype=torch.int32, device=self.ens.device)
+            else:
+                if self.mtab is None:
+                    self.mtab = torch.empty(self.ens.nslots, dtype=torch.int32, device=self.ens.device)
+                with torch.cuda.stream(self.stream):  # ordered after the chunks that read the old table
+                    self.mtab[:len(slots)].copy_(torch.tensor(slots, dtype=torch.int32))
+                self.members = self.mtab[:len(slots)]
         k = min(chunk, min(r.nsteps - done for r, done in self.active.values()))
         with torch.cuda.stream(self.stream):
-            for _ in range(k):
-                self.ens.step(self.dt, self.members)
+            left = k
+            if not self.use_graphs or not self.ens._stepped:
+                n0 = k if not self.use_graphs else 1
+                for _ in range(n0):
+                    self.ens.step(self.dt, self.members)
+                left -= n0
+            for size in (16, 8, 4, 2, 1):
+                while left >= size:
+                    key = (len(slots), size, self.ens.curr)
+                    replay = self.graphs.get(key)
+                    if replay is None:
+                        replay = self.graphs[key] = self.ens.chunk_graph(self.dt, size, self.members, self.stream)
+                        self.captures += 1
+                    replay()
+                    self.replays += 1
+                    left -= size
             self.event = torch.cuda.Event()
             self.event.record(self.stream)
         for st in self.active.values():
@@ -161,14 +194,20 @@ class _Pool:
 
 class Server:
     def __init__(self, cfg: DDCConfig = None, device="cuda:0", slots_per_block=16, max_slots=256,
-                 reserve_bytes=2 << 30):
+                 reserve_bytes=2 << 30, graphs=True):
         self.cfg = cfg or DDCConfig()
+        self.use_graphs = bool(graphs)  # replay chunks as captured CUDA graphs
         self.device = torch.device(device)
         self.slots_per_block = slots_per_block
         self.max_slots = max_slots
         self.reserve = reserve_bytes
         self.pools = {}
         self.refused = 0  # admissions deferred for lack of memory
+
+    def graph_stats(self):
+        """Chunk graphs captured and replayed over all pools."""
+        return {"captures": sum(p.captures for p in self.pools.values()),
+                "replays": sum(p.replays for p in self.pools.values())}
 
     def _pool_for(self, req):
         key = (req.nx, req.nz)

@@ -56,6 +56,29 @@ def test_result_same_alone_and_in_mix(cuda):
     assert all(r.admitted < target2.admitted < target2.finished < r.finished for r in same)
 
 
+def test_chunk_graphs_match_per_step_launches(cuda):
+    """Chunks replayed as captured graphs (over a member table rewritten as
+    requests join and leave, and a pool that grows) give every request the
+    same bits as launching each step from the host."""
+    from melvin.serving import Request, Server
+
+    def reqs():
+        return [Request(rid=i, nx=nx, nz=nz, r_rho=1.5 + 0.25 * i, nsteps=n, arrival=a, seed=50 + i)
+                for i, (nx, nz, n, a) in enumerate([(64, 33, 37, 0.0), (64, 33, 21, 0.002), (32, 17, 45, 0.0),
+                                                    (64, 33, 50, 0.004), (64, 33, 19, 0.006), (32, 17, 3, 0.01)])]
+
+    runs = {}
+    for graphs in (False, True):
+        srv = Server(_cfg("split"), slots_per_block=2, graphs=graphs)
+        out = srv.run(reqs(), keep_results=True, time_fn=StepClock())
+        runs[graphs] = ({r.rid: r.result for r in out}, srv.graph_stats())
+    for rid, res in runs[False][0].items():
+        assert np.array_equal(res, runs[True][0][rid]), rid
+    assert runs[False][1] == {"captures": 0, "replays": 0}
+    st = runs[True][1]
+    assert st["captures"] > 0 and st["replays"] > st["captures"], st
+
+
 def test_served_result_matches_oracle(cuda):
     from melvin.serving import Request, Server
 
