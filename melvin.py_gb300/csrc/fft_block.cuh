@@ -267,12 +267,28 @@ __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c
 // (16 or 8).  The tail avoids a radix-2 pass: with RM = 8 a remaining length
 // of 16 is split 4 x 4 rather than 8 x 2, with RM = 16 a remaining 32 is
 // split 8 x 4 rather than 16 x 2.
+__host__ __device__ constexpr int pass_radix(int N, int NS, int RM) {
+  return (RM >= 16 && N / NS >= 16 && N / NS != 32) ? 16
+                                                    : ((N / NS >= 8 && N / NS != 16) ? 8 : (N / NS >= 4 ? 4 : 2));
+}
 template <int N, int NS, int RM>
 struct PassRadix {
-  static constexpr int rem = N / NS;
-  static constexpr int value = (RM >= 16 && rem >= 16 && rem != 32)
-                                   ? 16
-                                   : ((rem >= 8 && rem != 16) ? 8 : (rem >= 4 ? 4 : 2));
+  static constexpr int value = pass_radix(N, NS, RM);
+};
+
+// First sub-transform length at or after NS whose pass is not radix 8.
+__host__ __device__ constexpr int radix8_run_end(int N, int NS, int RM) {
+  while (NS < N && pass_radix(N, NS, RM) == 8) NS *= 8;
+  return NS;
+}
+
+// Double-float passes are long (about 700 FP32 instructions per twiddled
+// radix-8 butterfly); its consecutive twiddled radix-8 passes share one copy
+// of the code, looped over a runtime sub-transform length, so that the
+// kernels' code fits the instruction caches better.
+template <typename T>
+struct LoopedPasses {
+  static constexpr bool value = std::is_same<T, df64>::value;
 };
 
 // A pass's outputs as stored for the next pass: double-float values are
@@ -349,13 +365,61 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, const cx<T>* __restric
   __syncthreads();
 }
 
+// Twiddled radix-8 Stockham pass with a runtime sub-transform length ns
+// (a power of 8 times the first one, 1 < ns < N / 4): the same arithmetic
+// as stockham_pass<..., 8, NS>.
+template <typename T, int N, int C, int CS, int NT, int DIR>
+__device__ __forceinline__ void stockham_pass8_rt(cx<T>* buf, const cx<T>* __restrict__ tw, int ns) {
+  constexpr int R = 8;
+  constexpr int NB = C * (N / R);
+  constexpr int BPT = (NB + NT - 1) / NT;
+  const int tws = N / (R * ns);
+  cx<T> v[BPT][R];
+#pragma unroll
+  for (int t = 0; t < BPT; ++t) {
+    const int b = threadIdx.x + t * NT;
+    if (NB % NT == 0 || b < NB) {
+      const int c = b % C, i = b / C;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[t][r] = buf[sx<T, CS>(i + r * (N / R), c)];
+      const int k = i & (ns - 1);
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        const cx<T> w = tw[r * k * tws];
+        v[t][r] = DIR < 0 ? cmul(v[t][r], w) : cmulc(v[t][r], w);
+      }
+      Dft<R, DIR, T>::run(v[t]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < BPT; ++t) {
+    const int b = threadIdx.x + t * NT;
+    if (NB % NT == 0 || b < NB) {
+      const int c = b % C, i = b / C;
+      const int k = i & (ns - 1);
+      const int base = (i - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) buf[sx<T, CS>(base + r * ns, c)] = pass_out(v[t][r]);
+    }
+  }
+  __syncthreads();
+}
+
 template <typename T, int N, int C, int CS, int NT, int DIR, int RM, int NS, bool ZB = false,
           bool DONE = (NS >= N)>
 struct FftPasses {
   static __device__ __forceinline__ void run(cx<T>* buf, const cx<T>* __restrict__ tw) {
     constexpr int R = PassRadix<N, NS, RM>::value;
-    stockham_pass<T, N, C, CS, NT, DIR, R, NS, ZB && NS == 1>(buf, tw);
-    FftPasses<T, N, C, CS, NT, DIR, RM, NS * R>::run(buf, tw);
+    constexpr int END = radix8_run_end(N, NS, RM);
+    if constexpr (LoopedPasses<T>::value && NS > 1 && R == 8 && END > NS * 8) {
+#pragma unroll 1
+      for (int ns = NS; ns < END; ns *= 8) stockham_pass8_rt<T, N, C, CS, NT, DIR>(buf, tw, ns);
+      FftPasses<T, N, C, CS, NT, DIR, RM, END>::run(buf, tw);
+    } else {
+      stockham_pass<T, N, C, CS, NT, DIR, R, NS, ZB && NS == 1>(buf, tw);
+      FftPasses<T, N, C, CS, NT, DIR, RM, NS * R>::run(buf, tw);
+    }
   }
 };
 
