@@ -267,29 +267,35 @@ __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c
 // (16 or 8).  The tail avoids a radix-2 pass: with RM = 8 a remaining length
 // of 16 is split 4 x 4 rather than 8 x 2, with RM = 16 a remaining 32 is
 // split 8 x 4 rather than 16 x 2.
-__host__ __device__ constexpr int pass_radix(int N, int NS, int RM) {
-  return (RM >= 16 && N / NS >= 16 && N / NS != 32) ? 16
-                                                    : ((N / NS >= 8 && N / NS != 16) ? 8 : (N / NS >= 4 ? 4 : 2));
-}
-template <int N, int NS, int RM>
-struct PassRadix {
-  static constexpr int value = pass_radix(N, NS, RM);
-};
-
-// First sub-transform length at or after NS whose pass is not radix 8.
-__host__ __device__ constexpr int radix8_run_end(int N, int NS, int RM) {
-  while (NS < N && pass_radix(N, NS, RM) == 8) NS *= 8;
-  return NS;
-}
-
 // Double-float passes are long (about 700 FP32 instructions per twiddled
-// radix-8 butterfly); its consecutive twiddled radix-8 passes share one copy
-// of the code, looped over a runtime sub-transform length, so that the
-// kernels' code fits the instruction caches better.
+// radix-8 butterfly).  Its transforms with maximum radix 8 put the radix-4
+// passes first (2048 = 4 x 8 x 8 x 8) and run the radix-8 passes that follow
+// as one copy of the code, looped over a runtime sub-transform length, so
+// that the kernels' code fits the instruction caches.
 template <typename T>
 struct LoopedPasses {
   static constexpr bool value = std::is_same<T, df64>::value;
 };
+
+__host__ __device__ constexpr int pass_radix(int N, int NS, int RM, bool small_first = false) {
+  if (small_first && RM == 8) {
+    // log2 N mod 3 = 0: all radix 8; 2: one radix-4 pass first; 1: two
+    const int L = ilog2c(N), lead = L % 3 == 0 ? 0 : (L % 3 == 2 ? 1 : 2);
+    return ilog2c(NS) < 2 * lead ? 4 : 8;
+  }
+  return (RM >= 16 && N / NS >= 16 && N / NS != 32) ? 16
+                                                    : ((N / NS >= 8 && N / NS != 16) ? 8 : (N / NS >= 4 ? 4 : 2));
+}
+template <typename T, int N, int NS, int RM>
+struct PassRadix {
+  static constexpr int value = pass_radix(N, NS, RM, LoopedPasses<T>::value);
+};
+
+// First sub-transform length at or after NS whose pass is not radix 8.
+__host__ __device__ constexpr int radix8_run_end(int N, int NS, int RM, bool small_first) {
+  while (NS < N && pass_radix(N, NS, RM, small_first) == 8) NS *= 8;
+  return NS;
+}
 
 // A pass's outputs as stored for the next pass: double-float values are
 // renormalised (df_renorm), so the unnormalised low words that additions
@@ -303,12 +309,12 @@ __device__ __forceinline__ cx<df64> pass_out(cx<df64> v) {
   return mk(df_renorm(v.x), df_renorm(v.y));
 }
 
-// Whether the first pass of a length-N transform with maximum radix RM
+// Whether the first pass of a length-N transform of T with maximum radix RM
 // skips the inputs 3N/8 .. 5N/8 - 1 when the caller marks them zero (ZB):
 // only a radix-8 first pass does, and the caller then need not fill them.
-template <int N, int RM, bool ZB>
+template <typename T, int N, int RM, bool ZB>
 struct ZeroBand {
-  static constexpr bool value = ZB && PassRadix<N, 1, RM>::value == 8;
+  static constexpr bool value = ZB && PassRadix<T, N, 1, RM>::value == 8;
 };
 
 template <typename T, int N, int C, int CS, int NT, int DIR, int R, int NS, bool ZB = false>
@@ -366,8 +372,7 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, const cx<T>* __restric
 }
 
 // Twiddled radix-8 Stockham pass with a runtime sub-transform length ns
-// (a power of 8 times the first one, 1 < ns < N / 4): the same arithmetic
-// as stockham_pass<..., 8, NS>.
+// (1 < ns <= N / 8): the same arithmetic as stockham_pass<..., 8, NS>.
 template <typename T, int N, int C, int CS, int NT, int DIR>
 __device__ __forceinline__ void stockham_pass8_rt(cx<T>* buf, const cx<T>* __restrict__ tw, int ns) {
   constexpr int R = 8;
@@ -410,8 +415,8 @@ template <typename T, int N, int C, int CS, int NT, int DIR, int RM, int NS, boo
           bool DONE = (NS >= N)>
 struct FftPasses {
   static __device__ __forceinline__ void run(cx<T>* buf, const cx<T>* __restrict__ tw) {
-    constexpr int R = PassRadix<N, NS, RM>::value;
-    constexpr int END = radix8_run_end(N, NS, RM);
+    constexpr int R = PassRadix<T, N, NS, RM>::value;
+    constexpr int END = radix8_run_end(N, NS, RM, LoopedPasses<T>::value);
     if constexpr (LoopedPasses<T>::value && NS > 1 && R == 8 && END > NS * 8) {
 #pragma unroll 1
       for (int ns = NS; ns < END; ns *= 8) stockham_pass8_rt<T, N, C, CS, NT, DIR>(buf, tw, ns);
@@ -436,7 +441,7 @@ template <typename T, int N, int C, int CS, int NT, int DIR, int RM = 8, bool ZB
 __device__ __forceinline__ void block_fft(cx<T>* buf, const cx<T>* __restrict__ tw) {
   static_assert((N & (N - 1)) == 0 && N >= 4, "power-of-two length");
   static_assert(RM == 16 || RM == 8, "maximum radix 16 or 8");
-  FftPasses<T, N, C, CS, NT, DIR, RM, 1, ZeroBand<N, RM, ZB>::value>::run(buf, tw);
+  FftPasses<T, N, C, CS, NT, DIR, RM, 1, ZeroBand<T, N, RM, ZB>::value>::run(buf, tw);
 }
 
 }  // namespace mgb

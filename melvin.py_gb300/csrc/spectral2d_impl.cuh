@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, sbuf_elems<T, C>(N) * sizeof(cx
   // zero the 2/3-rule gap rows nn+1 .. N-nn-1 (the kept rows are written
   // below), except 3N/8 .. 5N/8 - 1, which a pruned first pass does not read
   // (nn < 3N/8 holds for every fully spectral plan)
-  constexpr bool zb = ZeroBand<N, RM, true>::value;
+  constexpr bool zb = ZeroBand<T, N, RM, true>::value;
   constexpr int skip = zb ? N / 4 : 0;
   for (int e = threadIdx.x; e < (N - g.rows - skip) * C; e += NT) {
     const int x0 = g.nn + 1 + e / C, c = e % C;
@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
   // zero the modes nm .. N-nm of the input columns (the rest is written
   // below), except 3N/8 .. 5N/8 - 1, which a pruned first pass does not read
   // (nm <= 3N/8 holds for every fully spectral plan)
-  constexpr bool zb = ZeroBand<N, RM, true>::value;
+  constexpr bool zb = ZeroBand<T, N, RM, true>::value;
   constexpr int skip = zb ? N / 4 : 0;
   for (int e = threadIdx.x; e < (N - 2 * nm + 1 - skip) * P * NIN; e += NT) {
     const int z0 = nm + e / (P * NIN), c = e % (P * NIN);
