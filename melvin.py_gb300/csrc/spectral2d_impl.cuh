@@ -21,9 +21,10 @@
 // relatives in three HBM round trips.  The finite-difference stencils of
 // vec_dot_nabla (melvin/Variable.py:119-128,
 // melvin/SpatialDifferentiator.py:76-185) are applied in the pass that holds
-// the full periodic line: d/dz of uz*q along each row inside k_zz_step, and
-// d/dx of (ux*q)^ along each column inside k_xf_step (the z transform is
-// linear and commutes with the x stencil).
+// the full periodic line: d/dz of uz*q inside k_zz_step, as the stencil's
+// Fourier symbol on the kept modes after the forward z transform (the same
+// circulant operator), and d/dx of (ux*q)^ along each column inside
+// k_xf_step (the z transform is linear and commutes with the x stencil).
 #pragma once
 
 #include "fft_block.cuh"
