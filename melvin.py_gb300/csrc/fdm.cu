@@ -119,6 +119,9 @@ int thomas(const mgb_plan* p, Mptr rhs, double sign, Mptr out, const int* member
 
 int fd_plan_init(mgb_plan* p) {
   const GridC& g = p->g;
+  // The inverse x transforms skip the inputs 3N/8 .. 5N/8 - 1 as removed
+  // modes: true of the 2/3 rule (nn = (nx - 1) / 3).
+  if (8 * g.nn > 3 * g.nx) return MGB_ERR_INVALID;
   const size_t n = (size_t)g.nn * g.nz;
   std::vector<double> ip(n, 0.0), cp(n, 0.0), ps(n, 0.0), qs(n, 0.0);
   const double a = 1.0 / (g.dz * g.dz);

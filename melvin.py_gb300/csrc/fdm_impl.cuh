@@ -393,7 +393,8 @@ __global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
     }
   }
   __syncthreads();
-  block_fft<T, N, CP, CP, NT, +1>(buf, (const cx<T>*)a.tw);
+  // modes nn .. N-nn are zero (the 2/3 rule: nn <= 3N/8)
+  block_fft<T, N, CP, CP, NT, +1, 8, true>(buf, (const cx<T>*)a.tw);
   T* out = (T*)maddr(jb.phys, a.members, blockIdx.z);
   for (int e = threadIdx.x; e < N * CP; e += NT) {
     const int x = e / CP, j = e - x * CP;
