@@ -324,6 +324,16 @@ int mgb_step_kernel_count(const mgb_plan* plan, const mgb_equation* eq, int32_t*
 int mgb_step_events(const mgb_plan* plan, const mgb_equation* eq, void* const* q, void* const* hist,
                     int32_t curr, double dt, void* work, double* diag, void* stream,
                     void* const* events, int32_t nevents);
+/* mgb_step whose kernel k first makes `stream` wait for the caller-created
+ * CUDA event waits[k] (k < nwaits; NULL entries: no wait).  Data that only
+ * a later kernel reads can then arrive on another stream while the earlier
+ * kernels run: the history slots are read only by the update, kernel 2 of
+ * every step (the forward x pass; on FDM-z plans the forward x pass of the
+ * first stage).  No reference counterpart (the reference's arrays are
+ * host-resident). */
+int mgb_step_waits(const mgb_plan* plan, const mgb_equation* eq, void* const* q, void* const* hist,
+                   int32_t curr, double dt, void* work, double* diag, void* stream,
+                   void* const* waits, int32_t nwaits);
 
 /* Throughput probe of the FP64 FMA pipe (the denominator of the FP64-ALU
  * roofline of the FP64 step): launches `blocks` CTAs whose threads run

@@ -576,6 +576,16 @@ int mgb_step_events(const mgb_plan* p, const mgb_equation* eq, void* const* q, v
   return step_impl(p, eq, q, hist, curr, dt, work, diag, stream, &et);
 }
 
+int mgb_step_waits(const mgb_plan* p, const mgb_equation* eq, void* const* q, void* const* hist, int32_t curr,
+                   double dt, void* work, double* diag, void* stream, void* const* waits, int32_t nwaits) {
+  CHECK_PTR(waits);
+  if (nwaits < 0) return fail(MGB_ERR_INVALID, "mgb_step_waits: nwaits=%d", nwaits);
+  EventTrack et;
+  et.wait = (const cudaEvent_t*)waits;
+  et.nwait = nwaits;
+  return step_impl(p, eq, q, hist, curr, dt, work, diag, stream, &et);
+}
+
 static int check_run_config(const mgb_run_config* cfg, const char* fn) {
   if (cfg->horizon < 1) return fail(MGB_ERR_INVALID, "%s: horizon=%d (>= 1)", fn, cfg->horizon);
   if (cfg->cfl_cadence < 0 || cfg->tracker_cadence < 0 || cfg->capacity < 0)

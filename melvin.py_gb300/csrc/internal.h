@@ -97,14 +97,18 @@ int fs_vec_dot_nabla(const mgb_plan* p, const zd* q, double* q_phys, const doubl
                      const double* uz, zd* out, void* work, cudaStream_t s);
 int fs_velocity(const mgb_plan* p, const zd* w, zd* psi, zd* ux_s, zd* uz_s, double* ux,
                 double* uz, void* work, cudaStream_t s);
-// Optional per-kernel timing: ev[0] is recorded before the first kernel and
-// ev[k] after kernel k, for k < nev.
+// Optional per-kernel events: ev[0] is recorded before the first kernel and
+// ev[k] after kernel k, for k < nev; kernel k waits for wait[k] (when not
+// null, k < nwait) before it starts.
 struct EventTrack {
   cudaEvent_t* ev = nullptr;
   int nev = 0;
+  const cudaEvent_t* wait = nullptr;
+  int nwait = 0;
   int k = 0;
   void mark(cudaStream_t s) {
     if (ev && k < nev) cudaEventRecord(ev[k], s);
+    if (wait && k < nwait && wait[k]) cudaStreamWaitEvent(s, wait[k], 0);
     ++k;
   }
 };

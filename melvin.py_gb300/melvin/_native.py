@@ -190,6 +190,8 @@ SIGNATURES = {
     "mgb_step_kernel_count": [_P, C.POINTER(MgbEquation), C.POINTER(_I)],
     "mgb_step_events": [_P, C.POINTER(MgbEquation), C.POINTER(_P), C.POINTER(_P), _I, _D, _P, _P, _P,
                         C.POINTER(_P), _I],
+    "mgb_step_waits": [_P, C.POINTER(MgbEquation), C.POINTER(_P), C.POINTER(_P), _I, _D, _P, _P, _P,
+                       C.POINTER(_P), _I],
     "mgb_run_begin": [_P, _P, C.POINTER(MgbRunConfig), _P],
     "mgb_run_step": [_P, C.POINTER(MgbEquation), C.POINTER(_P), C.POINTER(_P), _I, C.c_int64, _I, _P, _P,
                      C.POINTER(MgbRunConfig), _P],

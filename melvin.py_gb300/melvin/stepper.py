@@ -155,3 +155,54 @@ class Stepper:
             N.stream_handle(self.device), ev, len(events)))
         for f in self.fields:
             f.dvar.advance()
+
+    def step_host(self, states, histories, dt=None):
+        """One step of fields whose state and history live in host memory.
+
+        ``states[i]`` and ``histories[i]`` are pinned CPU tensors shaped like
+        field i's state and history (the device tensors are the staging
+        copies).  On the current stream the states go up, the step runs, and
+        the states and the history slot the step writes come back.  The
+        history slots the update reads go up on a second stream, and the
+        update (kernel 2, mgb_step_waits) waits for them, so that upload
+        overlaps the transforms; the slot the step overwrites whole is not
+        uploaded.  Fully spectral plans.  Returns the bytes copied up and
+        down; the host tensors hold the result once the current stream has
+        passed this point."""
+        if self.plan.grid.fdm_z:
+            raise NotImplementedError("step_host: fully spectral plans only")
+        dt = self.sim._integrator._dt if dt is None else dt
+        self._ensure(dt)
+        main = torch.cuda.current_stream(self.device)
+        if getattr(self, "_copy_stream", None) is None:
+            self._copy_stream = torch.cuda.Stream(device=self.device)
+            self._hist_ready = torch.cuda.Event()
+        cs = self._copy_stream
+        curr = self.fields[0].dvar._curr_idx
+        order = self.fields[0].dvar._data.shape[0]
+        read = [s for s in range(order) if s != curr]
+        up = down = 0
+        cs.wait_stream(main)  # the previous download into these host tensors has finished
+        with torch.cuda.stream(cs):
+            for f, h in zip(self.fields, histories):
+                for s in read:
+                    f.dvar._data[s].copy_(h[s], non_blocking=True)
+                    up += h[s].numel() * h.element_size()
+            self._hist_ready.record(cs)
+        for i, (f, h) in enumerate(zip(self.fields, states)):
+            if f.dvar._curr_idx != curr:
+                raise ValueError("all histories of a fused step must share curr_idx")
+            f.var._sdata.copy_(h, non_blocking=True)
+            up += h.numel() * h.element_size()
+            self._q[i] = f.var._sdata.data_ptr()
+            self._h[i] = f.dvar._data.data_ptr()
+        waits = (C.c_void_p * 3)(None, None, self._hist_ready.cuda_event)
+        N.check(self.plan.lib.mgb_step_waits(
+            self.plan.handle, C.byref(self.eq), self._q, self._h, curr, float(dt), N.ptr(self.work), None,
+            N.stream_handle(self.device), waits, 3))
+        for f, hs, hh in zip(self.fields, states, histories):
+            hs.copy_(f.var._sdata, non_blocking=True)
+            hh[curr].copy_(f.dvar._data[curr], non_blocking=True)
+            down += hs.numel() * hs.element_size() + hh[curr].numel() * hh.element_size()
+            f.dvar.advance()
+        return up, down

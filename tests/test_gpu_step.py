@@ -221,3 +221,35 @@ def test_fused_step_large_grids(cuda, nx, nz, fdm, precision, integ, order, tol)
             step.step()
             ref.step()
         assert rel_l2(w.gets().cpu().numpy(), ref.q[0]) < tol
+
+
+@pytest.mark.parametrize("tag", ["tg32_o2_ab2", "tg32_o4_ab4", "kh64x32"])
+def test_step_host_matches_device_step(cuda, golden, tag):
+    """Stepper.step_host (state and history in pinned host memory, only the
+    read history slots uploaded, on a second stream that the update waits
+    for) leaves the host tensors bit-identical to the device-resident step,
+    history included, over steps that cycle through every history slot."""
+    g, specs, names, integ, order, dt = TRAJ_CASES[tag]
+    runs = []
+    for _ in range(2):
+        sim, p, V, D, bf = build(g, names, integ, order, dt)
+        for n in names:
+            V[n].sets(golden[f"{tag}/s0_{n}"])
+        runs.append((V, D, stepper_for(tag, sim, V, D, integ)))
+    (Va, Da, sa), (Vb, Db, sb) = runs
+    hs = [Vb[n]._sdata.cpu().pin_memory() for n in names]
+    hh = [Db[n]._data.cpu().pin_memory() for n in names]
+    for n in names:  # the device staging copies start stale: only the host tensors are the state
+        Vb[n]._sdata.zero_()
+        Db[n]._data.fill_(float("nan"))
+    nsteps = 2 * order + 1
+    for _ in range(nsteps):
+        sa.step(dt)
+        up, down = sb.step_host(hs, hh, dt)
+    torch.cuda.synchronize()
+    S = Va[names[0]]._sdata.numel() * 16
+    assert up == len(names) * order * S and down == 2 * len(names) * S, (up, down)
+    for i, n in enumerate(names):
+        assert torch.equal(hs[i], Va[n]._sdata.cpu()), n
+        assert torch.equal(hh[i], Da[n]._data.cpu()), n
+        assert Db[n]._curr_idx == Da[n]._curr_idx
