@@ -133,6 +133,19 @@ __device__ __forceinline__ cx<To> cvt(cx<From> a) {
   return mk(Cvt<To, From>::run(a.x), Cvt<To, From>::run(a.y));
 }
 
+// A double kernel argument (a grid constant, a stencil or scale factor) in
+// the kernel's arithmetic type T, through the same integer-pipe conversions:
+// every thread converts its constants, and the hardware conversion would
+// take FP64-pipe slots from the FP64 update that shares the kernel.
+template <typename T>
+__device__ __forceinline__ T to_t(double v) {
+  if constexpr (std::is_same<T, double>::value) {
+    return v;
+  } else {
+    return Cvt<T, double>::run(v);
+  }
+}
+
 // Shared-memory FFT buffers of complex T hold column c of row x at
 // x*CS + c + (x/8)*PAD.  The padding breaks the bank conflicts of the
 // strided Stockham accesses (the first pass stores rows 8 apart; a block

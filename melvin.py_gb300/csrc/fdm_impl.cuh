@@ -311,7 +311,7 @@ __device__ __forceinline__ zd fd_snabla2_t(const GridC& g, const zd* row, int n,
             inv;
     }
   }
-  const T f = (T)g.d2x * (T)(n * n);
+  const T f = to_t<T>(g.d2x) * (T)(n * n);
   return cvt<double>((q * f + acc) * kappa);
 }
 
@@ -372,21 +372,21 @@ __global__ void __launch_bounds__(NT) k_fd_xinv(const FdXinvArgs a) {
       // FP64 rows (the per-verb spec_out outputs are FP64-only)
       cx<T> A = mk<T>(0, 0), B = mk<T>(0, 0);
       if (jb.kind == FD_UX) {
-        const T inv = (T)a.fdz;
+        const T inv = to_t<T>(a.fdz);
         if (za < g.nz) A = -fd_ddz_row_t<T>(row, za, g.nz, g.sdo, inv);
         if (zb < g.nz) B = -fd_ddz_row_t<T>(row, zb, g.nz, g.sdo, inv);
       } else {
         if (za < g.nz) A = cvt<T>(row[za]);
         if (zb < g.nz) B = cvt<T>(row[zb]);
         if (jb.kind == FD_UZ) {
-          const T b = (T)g.dfx * (T)n;
+          const T b = to_t<T>(g.dfx) * (T)n;
           A = mk(-(b * A.y), b * A.x);
           B = mk(-(b * B.y), b * B.x);
         }
       }
       put_pair<T, N, CP>(buf, j, n, A, B);
       if (dout) {
-        const T kap = (T)jb.kappa, inv = (T)a.inv_dz2;
+        const T kap = to_t<T>(jb.kappa), inv = to_t<T>(a.inv_dz2);
         if (za < g.nz) dout[(size_t)n * g.nz + za] = fd_snabla2_t<T>(g, row, n, za, kap, inv);
         if (zb < g.nz) dout[(size_t)n * g.nz + zb] = fd_snabla2_t<T>(g, row, n, zb, kap, inv);
       }
@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(NT, (std::is_same<T, float>::value ? 8 : 1)) k
   const GridC& g = a.g;
   const int nx = g.nx, nz = g.nz, sdo = g.sdo, h = sdo / 2;
   const int x0 = blockIdx.y * FD_TX, z0 = blockIdx.x * FD_TZ;
-  const T fdx = (T)a.fdx, fdz = (T)a.fdz;
+  const T fdx = to_t<T>(a.fdx), fdz = to_t<T>(a.fdz);
   const T* ux = (const T*)maddr(a.ux, nullptr, blockIdx.z);
   const T* uz = (const T*)maddr(a.uz, nullptr, blockIdx.z);
   for (int e = threadIdx.x; e < SX * FD_TZ; e += NT) {

@@ -535,7 +535,7 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
   }
   block_fft<T, N, P * NOUT, CSO, NT, -1, RM>(buf, (const cx<T>*)a.tw);
   const cx<T>* twt = (const cx<T>*)a.tw;
-  const T fdz = (T)a.fdz;
+  const T fdz = to_t<T>(a.fdz);
   for (int m = threadIdx.x; m < nm; m += NT) {
     // c = d/dz b by the periodic stencil is the circulant whose symbol at
     // th = 2 pi m / N is i * sig, sig = 2 sin(th) fdz (order 2) or
@@ -651,7 +651,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, F * sbuf_elems<T, C>(N) * sizeo
   const GridC& g = a.g;
   const int m0 = blockIdx.x * C;
   const int sdo = g.sdo;
-  const T fdx = (T)a.fdx;
+  const T fdx = to_t<T>(a.fdx);
   const size_t moff = (size_t)blockIdx.y * a.b.inter_stride;
   const int mslot = batch_slot(a.b, blockIdx.y);
   // J_f = d/dx(A_f) + C_f: periodic x stencil along each column
@@ -695,7 +695,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, F * sbuf_elems<T, C>(N) * sizeo
   for (int f = 0; f < F; ++f) block_fft<T, N, C, C, NT, -1, RM>(buf + f * sbuf_elems<T, C>(N), (const cx<T>*)a.tw);
 
   // -1/(nx*nz) is a power of two for the grids built, so scaling in T is exact
-  const T neg_norm = (T)(-a.inv_norm);
+  const T neg_norm = to_t<T>(-a.inv_norm);
   const size_t slot = (size_t)g.rows * g.cols;
   zd* qf[F];
   zd* hf[F];
@@ -738,8 +738,6 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, F * sbuf_elems<T, C>(N) * sizeo
       if (e >= total || m >= g.cols) continue;
       const int n = row_mode(r, g.nn), k = row_bin(r, g.nn, N);
       const size_t idx = (size_t)r * g.cols + m;
-      zd psi = mk(0.0, 0.0);
-      if (a.need_psi) psi = mk(-(qo[u][0].x * rl[u]), -(qo[u][0].y * rl[u]));
 #pragma unroll
       for (int f = 0; f < F; ++f) {
         const XfField& eq = a.eq[f];
@@ -748,9 +746,12 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, F * sbuf_elems<T, C>(N) * sizeo
         zd fv = cvt<double>(J);
         for (int t = 0; t < eq.nterms; ++t) {
           const int sidx = eq.tsrc[t];
-          zd sv = psi;
+          // psi = -q_0 / lap, formed only for a term that reads it (computed
+          // ahead of the terms, the compiler made it unconditional: two FP64
+          // products per mode of every step)
+          zd sv = sidx < 0 ? mk(-(qo[u][0].x * rl[u]), -(qo[u][0].y * rl[u])) : qo[u][0];
 #pragma unroll
-          for (int q2 = 0; q2 < F; ++q2)
+          for (int q2 = 1; q2 < F; ++q2)
             if (sidx == q2) sv = qo[u][q2];
           const zd v = lin_term(g, sv, eq.top[t], n, m);
           const double cc = tco ? tco[f * 4 + t] : eq.tcoef[t];
