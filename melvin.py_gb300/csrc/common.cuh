@@ -134,15 +134,17 @@ __device__ __forceinline__ cx<To> cvt(cx<From> a) {
 }
 
 // A double kernel argument (a grid constant, a stencil or scale factor) in
-// the kernel's arithmetic type T, through the same integer-pipe conversions:
-// every thread converts its constants, and the hardware conversion would
-// take FP64-pipe slots from the FP64 update that shares the kernel.
+// the kernel's arithmetic type T.  FP32 goes through the integer-pipe
+// conversion: every thread converts its constants, and the hardware
+// conversion would take FP64-pipe slots from the FP64 update that shares
+// the kernel (split 2048^2 forward x pass 43.4 -> 39.0 us with the psi fix).
+// Double-float keeps its constructor (measured 1.5 us faster there).
 template <typename T>
 __device__ __forceinline__ T to_t(double v) {
-  if constexpr (std::is_same<T, double>::value) {
-    return v;
-  } else {
+  if constexpr (std::is_same<T, float>::value) {
     return Cvt<T, double>::run(v);
+  } else {
+    return T(v);
   }
 }
 
