@@ -357,6 +357,10 @@ int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
   za.partial = diag ? w.partial : nullptr;
   za.flux_f = eq->diag_flux - 1;
   za.fdz = fd_inv(g.sdo, g.dz);
+  // the forward x pass needs N = -J / (nx nz): the z pass leaves 2 A and
+  // -C / (nx nz), and the x stencil factor takes -1 / (2 nx nz)
+  const double out_scale = -0.5 / ((double)g.nx * (double)g.nz);
+  za.cscale = out_scale;
   za.tw = twz;
   st = launched(Lz->zz_step[prec][F - 1][tile[MGB_FAMILY_ZSTEP]](za, nb, s), "step z pass");
   if (st) return st;
@@ -387,8 +391,7 @@ int fs_batch_step(const mgb_plan* p, const mgb_equation* eq, const StepBatch& sb
   fa.order = eq->order;
   fa.curr = curr;
   fa.integrator = eq->integrator;
-  fa.fdx = fd_inv(g.sdo, g.dx);
-  fa.inv_norm = 1.0 / ((double)g.nx * (double)g.nz);
+  fa.fdx = fd_inv(g.sdo, g.dx) * out_scale;
   fa.tw = twx;
   st = launched(Lx->xf_step[prec][F - 1][tile[MGB_FAMILY_XFWD]](fa, nb, s), "step forward x pass");
   if (st) return st;

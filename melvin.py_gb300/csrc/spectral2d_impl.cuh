@@ -259,14 +259,20 @@ __device__ __forceinline__ void put_pair(cx<T>* buf, int col, int m, cx<T> A, cx
   }
 }
 
-// Split the forward transform Z of a + i b into the half spectra of a and b.
-template <typename T, int N, int CS>
+// Split the forward transform Z of a + i b into the half spectra of a and b
+// (HALF = false: twice them, the factor 1/2 left to the caller).
+template <typename T, int N, int CS, bool HALF = true>
 __device__ __forceinline__ void get_pair(const cx<T>* buf, int col, int m, cx<T>& A, cx<T>& B) {
   const cx<T> zm = buf[sx<T, CS>(m, col)];
   const cx<T> zn = buf[sx<T, CS>((N - m) & (N - 1), col)];
-  const T h = (T)0.5;
-  A = mk((zm.x + zn.x) * h, (zm.y - zn.y) * h);
-  B = mk((zm.y + zn.y) * h, (zn.x - zm.x) * h);
+  if constexpr (HALF) {
+    const T h = (T)0.5;
+    A = mk((zm.x + zn.x) * h, (zm.y - zn.y) * h);
+    B = mk((zm.y + zn.y) * h, (zn.x - zm.x) * h);
+  } else {
+    A = mk(zm.x + zn.x, zm.y - zn.y);
+    B = mk(zm.y + zn.y, zn.x - zm.x);
+  }
 }
 
 // Periodic central first difference of the imaginary parts of column `col`
@@ -352,6 +358,11 @@ __device__ __forceinline__ void block_diag(double s, double mx, double mz, doubl
 //   a_f = ux * q_f, b_f = uz * q_f, forward r2c of a_f + i b_f, keep the nm
 //   leading modes, C_f = d/dz B_f (the periodic stencil applied as its
 //   Fourier symbol: the same circulant operator, only rounding differs).
+// The outputs are scaled for the forward x pass: 2 A_f and -C_f / (nx nz)
+// (cscale = -1 / (2 nx nz) multiplies the symbol); the x pass's stencil
+// factor carries the matching -1 / (2 nx nz), so N = -J / (nx nz) costs no
+// product per mode.  All three factors are powers of two: the results are
+// those of the unscaled form.
 // Pair p's inputs sit in columns p*NIN + i and its outputs in p*NOUT + j of
 // the CTA's buffer; a thread reads every input of a position z before it
 // writes that position's outputs.  Outputs may alias the inputs: a CTA reads
@@ -369,6 +380,7 @@ struct ZzArgs {
   double* partial;    // optional [member][gridDim.x][kDiagW]
   int flux_f;         // field whose sum of uz * q the partials carry (-1: none)
   double fdz;         // 1/(2dz) or 1/(3dz)
+  double cscale;      // -1 / (2 nx nz): scale of the C outputs' symbol
   const void* tw;
   BatchC b;           // member = blockIdx.y
 };
@@ -535,13 +547,13 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
   }
   block_fft<T, N, P * NOUT, CSO, NT, -1, RM>(buf, (const cx<T>*)a.tw);
   const cx<T>* twt = (const cx<T>*)a.tw;
-  const T fdz = to_t<T>(a.fdz);
+  const T fdz = to_t<T>(a.fdz), cscale = to_t<T>(a.cscale);
   for (int m = threadIdx.x; m < nm; m += NT) {
     // c = d/dz b by the periodic stencil is the circulant whose symbol at
     // th = 2 pi m / N is i * sig, sig = 2 sin(th) fdz (order 2) or
     // (4 sin(th) - sin(2 th) / 2) fdz (order 4), with tw[t] = exp(-2 pi i t / N)
     const T s1 = -twt[m].y;
-    const T sig = g.sdo == 2 ? (T)2 * s1 * fdz : ((T)4 * s1 - (T)0.5 * (-twt[2 * m].y)) * fdz;
+    const T sig = (g.sdo == 2 ? (T)2 * s1 * fdz : ((T)4 * s1 - (T)0.5 * (-twt[2 * m].y)) * fdz) * cscale;
 #pragma unroll
     for (int p = 0; p < P; ++p) {
       const size_t r0 = (size_t)(xb + 2 * p) * ld, r1 = r0 + ld;
@@ -552,7 +564,7 @@ __global__ void __launch_bounds__(NT, (ZzOcc<T, N, F, P, RM>::value))
 #pragma unroll
         for (int rho = 0; rho < 2; ++rho) {
           cx<T> A, B;
-          get_pair<T, N, CSO>(buf, p * NOUT + rho * F + f, m, A, B);
+          get_pair<T, N, CSO, false>(buf, p * NOUT + rho * F + f, m, A, B);
           ao[(rho ? r1 : r0) + m] = A;
           co[(rho ? r1 : r0) + m] = mk(-(sig * B.y), sig * B.x);
         }
@@ -589,7 +601,7 @@ struct XfArgs {
   const zd* coef[3];   // per-mode update coefficients (a, b) from mgb_step_prepare
   const double* rlap;  // 1/lap, for linear terms of psi
   int order, curr, integrator, need_psi;
-  double fdx, inv_norm;
+  double fdx;          // stencil factor 1/(2dx) or 1/(3dx) times -1/(2 nx nz) (the z pass's scaling)
   XfField eq[3];
   const void* tw;
   BatchC b;            // member = blockIdx.y
@@ -695,7 +707,6 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, F * sbuf_elems<T, C>(N) * sizeo
   for (int f = 0; f < F; ++f) block_fft<T, N, C, C, NT, -1, RM>(buf + f * sbuf_elems<T, C>(N), (const cx<T>*)a.tw);
 
   // -1/(nx*nz) is a power of two for the grids built, so scaling in T is exact
-  const T neg_norm = to_t<T>(-a.inv_norm);
   const size_t slot = (size_t)g.rows * g.cols;
   zd* qf[F];
   zd* hf[F];
@@ -742,7 +753,7 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, F * sbuf_elems<T, C>(N) * sizeo
       for (int f = 0; f < F; ++f) {
         const XfField& eq = a.eq[f];
         // dq[:] = -q.vec_dot_nabla(...) + linear terms
-        const cx<T> J = buf[f * sbuf_elems<T, C>(N) + sx<T, C>(k, c)] * neg_norm;
+        const cx<T> J = buf[f * sbuf_elems<T, C>(N) + sx<T, C>(k, c)];  // already -J / (nx nz)
         zd fv = cvt<double>(J);
         for (int t = 0; t < eq.nterms; ++t) {
           const int sidx = eq.tsrc[t];

@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(ZrShape<N>::NTZ, (ZrOcc<N, F>::value)) k_zz_re
   }
   __syncthreads();
   if (live) {
-    const float inv = (float)a.fdz;
+    const float inv = to_t<float>(a.fdz), cscale = to_t<float>(a.cscale);
     const size_t r0 = (size_t)x0 * ld, r1 = r0 + ld;
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
@@ -339,13 +339,15 @@ __global__ void __launch_bounds__(ZrShape<N>::NTZ, (ZrOcc<N, F>::value)) k_zz_re
       if (m < nm) {
         // FD symbol: sigma = 2 sin(th) inv (order 2), (4 sin th - sin(2th)/2) inv (order 4)
         const float s1 = -ldg_cx(tw + m).y;
-        const float sig = g.sdo == 2 ? 2.f * s1 * inv : (4.f * s1 - 0.5f * -ldg_cx(tw + ((2 * m) & (N - 1))).y) * inv;
+        const float sig =
+            (g.sdo == 2 ? 2.f * s1 * inv : (4.f * s1 - 0.5f * -ldg_cx(tw + ((2 * m) & (N - 1))).y) * inv) * cscale;
 #pragma unroll
         for (int o = 0; o < NOUT; ++o) {
           const cx<float> zm = v[o][s];
           const cx<float> zn = m == 0 ? zm : buf[o * N + zsw(N - m)];
-          const cx<float> A = mk((zm.x + zn.x) * 0.5f, (zm.y - zn.y) * 0.5f);
-          const cx<float> B = mk((zm.y + zn.y) * 0.5f, (zn.x - zm.x) * 0.5f);
+          // 2 A and 2 B: the factor 1/2 is in the scales (see ZzArgs)
+          const cx<float> A = mk(zm.x + zn.x, zm.y - zn.y);
+          const cx<float> B = mk(zm.y + zn.y, zn.x - zm.x);
           const int f = o < F ? o : o - F;
           const size_t rr = o < F ? r0 : r1;
           cx<float>* ao = (cx<float>*)((char*)a.aout[f] + moff);
