@@ -425,6 +425,17 @@ struct FdPhysArgs {
   Gate gate;
 };
 
+// Central first difference (-f[i+2]/4 + 2 f[i+1] - 2 f[i-1] + f[i-2]/4) * inv
+// of order 4 (inv = 1/(3h)), or (f[i+1] - f[i-1]) * inv of order 2, as
+// (p1 - m1) * inv2 - (p2 - m2) * inv4 with inv2 = 2 inv, inv4 = inv / 4: four
+// operations instead of five (powers of two, so inv2 and inv4 are exact).
+template <typename T>
+__device__ __forceinline__ T st1(T p2, T p1, T m1, T m2, int sdo, T inv, T inv2, T inv4) {
+  if (sdo == 2) return (p1 - m1) * inv;
+  return (p1 - m1) * inv2 - (p2 - m2) * inv4;
+}
+// The same difference in the reference's order of operations
+// (melvin/SpatialDifferentiator.py:76-104; the per-verb kernels).
 template <typename T>
 __device__ __forceinline__ T st1(T p2, T p1, T m1, T m2, int sdo, T inv) {
   if (sdo == 2) return (p1 - m1) * inv;
@@ -453,6 +464,7 @@ __global__ void __launch_bounds__(NT, (std::is_same<T, float>::value ? 8 : 1)) k
   const int nx = g.nx, nz = g.nz, sdo = g.sdo, h = sdo / 2;
   const int x0 = blockIdx.y * FD_TX, z0 = blockIdx.x * FD_TZ;
   const T fdx = to_t<T>(a.fdx), fdz = to_t<T>(a.fdz);
+  const T fdx2 = fdx * (T)2, fdx4 = fdx * (T)0.25, fdz2 = fdz * (T)2, fdz4 = fdz * (T)0.25;
   const T* ux = (const T*)maddr(a.ux, nullptr, blockIdx.z);
   const T* uz = (const T*)maddr(a.uz, nullptr, blockIdx.z);
   for (int e = threadIdx.x; e < SX * FD_TZ; e += NT) {
@@ -515,15 +527,16 @@ __global__ void __launch_bounds__(NT, (std::is_same<T, float>::value ? 8 : 1)) k
       const int ii = i + H, kk = k + H;
       T jx, jz = 0;
       if constexpr (kStage) {
-        jx = st1(s_a[ii + 2][k], s_a[ii + 1][k], s_a[ii - 1][k], s_a[ii - 2][k], sdo, fdx);
-        if (z >= h && z < nz - h) jz = st1(s_b[i][kk + 2], s_b[i][kk + 1], s_b[i][kk - 1], s_b[i][kk - 2], sdo, fdz);
+        jx = st1(s_a[ii + 2][k], s_a[ii + 1][k], s_a[ii - 1][k], s_a[ii - 2][k], sdo, fdx, fdx2, fdx4);
+        if (z >= h && z < nz - h)
+          jz = st1(s_b[i][kk + 2], s_b[i][kk + 1], s_b[i][kk - 1], s_b[i][kk - 2], sdo, fdz, fdz2, fdz4);
       } else {
         const auto& s_q = s_b;
         jx = st1(s_ux[ii + 2][k] * s_q[ii + 2][kk], s_ux[ii + 1][k] * s_q[ii + 1][kk],
-                 s_ux[ii - 1][k] * s_q[ii - 1][kk], s_ux[ii - 2][k] * s_q[ii - 2][kk], sdo, fdx);
+                 s_ux[ii - 1][k] * s_q[ii - 1][kk], s_ux[ii - 2][k] * s_q[ii - 2][kk], sdo, fdx, fdx2, fdx4);
         if (z >= h && z < nz - h)
           jz = st1(s_uz[i][kk + 2] * s_q[ii][kk + 2], s_uz[i][kk + 1] * s_q[ii][kk + 1],
-                   s_uz[i][kk - 1] * s_q[ii][kk - 1], s_uz[i][kk - 2] * s_q[ii][kk - 2], sdo, fdz);
+                   s_uz[i][kk - 1] * s_q[ii][kk - 1], s_uz[i][kk - 2] * s_q[ii][kk - 2], sdo, fdz, fdz2, fdz4);
       }
       jo[(size_t)x * nz + z] = jx + jz;
     }
@@ -697,6 +710,7 @@ __global__ void __launch_bounds__(NT, (FdXfOcc<T, N, F, CP>::value)) k_fd_xfwd(c
   }
   const zd* psi = a.psi.base ? (const zd*)maddr(a.psi, a.members, zm) : nullptr;
   const double* tco = a.tcoef ? a.tcoef + (size_t)slot * 12 : nullptr;
+  const double hnx = 0.5 * a.inv_nx;
   for (int e = threadIdx.x; e < g.nn * C; e += NT) {
     const int n = e / C, c = e - n * C, z = z0 + c;
     if (z >= g.nz) continue;
@@ -722,12 +736,17 @@ __global__ void __launch_bounds__(NT, (FdXfOcc<T, N, F, CP>::value)) k_fd_xfwd(c
     }
 #pragma unroll
     for (int f = 0; f < F; ++f) {
-      cx<T> A, B;
-      get_pair<T, N, CP>(buf + f * sbuf_elems<T, CP>(N), j, n, A, B);
-      const zd v = cvt<double>(part ? B : A);
+      // column z's half spectrum, twice over: (Z(n) + conj Z(N-n)) for the
+      // even column of the pair, (Z(n) - conj Z(N-n)) / i for the odd one;
+      // the 1/2 rides on the 1/nx scale (a power of two: the same values)
+      const cx<T>* bf = buf + f * sbuf_elems<T, CP>(N);
+      const cx<T> zn = bf[sx<T, CP>(n, j)], zc = bf[sx<T, CP>((N - n) & (N - 1), j)];
+      const T s0 = part ? zn.y : zn.x, s1 = part ? zc.y : zc.x;
+      const T d0 = part ? zc.x : zn.y, d1 = part ? zn.x : zc.y;
+      const zd v = cvt<double>(mk(s0 + s1, d0 - d1));
       // f = -vec_dot_nabla + linear terms + diffusion (already in the slot)
       const zd d = hd[f];
-      zd fv = mk(d.x - v.x * a.inv_nx, d.y - v.y * a.inv_nx);
+      zd fv = mk(d.x - v.x * hnx, d.y - v.y * hnx);
       const FdXfField& eq = a.eq[f];
       for (int t = 0; t < eq.nterms; ++t) {
         const int sidx = eq.tsrc[t];
