@@ -263,10 +263,6 @@ __device__ __forceinline__ void dft8_zero34(cx<T>* a) {
 
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
-// Radix of the pass that starts with sub-transform length NS, at most RM
-// (16 or 8).  The tail avoids a radix-2 pass: with RM = 8 a remaining length
-// of 16 is split 4 x 4 rather than 8 x 2, with RM = 16 a remaining 32 is
-// split 8 x 4 rather than 16 x 2.
 // Double-float passes are long (about 700 FP32 instructions per twiddled
 // radix-8 butterfly).  Its transforms with maximum radix 8 put the radix-4
 // passes first (2048 = 4 x 8 x 8 x 8) and run the radix-8 passes that follow
@@ -277,6 +273,11 @@ struct LoopedPasses {
   static constexpr bool value = std::is_same<T, df64>::value;
 };
 
+// Radix of the pass that starts with sub-transform length NS, at most RM
+// (16 or 8).  The tail avoids a radix-2 pass: with RM = 8 a remaining length
+// of 16 is split 4 x 4 rather than 8 x 2, with RM = 16 a remaining 32 is
+// split 8 x 4 rather than 16 x 2.  small_first (double-float, RM = 8): the
+// radix-4 passes come first instead.
 __host__ __device__ constexpr int pass_radix(int N, int NS, int RM, bool small_first = false) {
   if (small_first && RM == 8) {
     // log2 N mod 3 = 0: all radix 8; 2: one radix-4 pass first; 1: two
