@@ -726,6 +726,7 @@ __global__ void __launch_bounds__(NT, (FdXfOcc<T, N, F, CP>::value)) k_fd_xfwd(c
     // every load of the element, for all fields, before the first store (the
     // compiler cannot reorder loads above stores through these pointers)
     zd qs[F], hd[F], q0[F], hp[F][3];
+    const double kx = g.dfx * (double)n;  // d/dx factor of the linear terms (every equation here has them)
     const zd ps = psi ? psi[idx] : mk(0.0, 0.0);
 #pragma unroll
     for (int f = 0; f < F; ++f) {
@@ -754,11 +755,11 @@ __global__ void __launch_bounds__(NT, (FdXfOcc<T, N, F, CP>::value)) k_fd_xfwd(c
 #pragma unroll
         for (int q2 = 1; q2 < F; ++q2)
           if (sidx == q2) sv = qs[q2];
-        if (eq.top[t] == 1) {
-          const double b = g.dfx * (double)n;
-          sv = mk(-(b * sv.y), b * sv.x);
+        double cc = tco ? tco[f * 4 + t] : eq.tcoef[t];
+        if (eq.top[t] == 1) {  // d/dx: the factor 2 pi n / lx rides on the coefficient, i on the value
+          cc *= kx;
+          sv = mk(-sv.y, sv.x);
         }
-        const double cc = tco ? tco[f * 4 + t] : eq.tcoef[t];
         fv = mk(fv.x + cc * sv.x, fv.y + cc * sv.y);
       }
       hf[f][(size_t)a.curr * hslot + idx] = fv;

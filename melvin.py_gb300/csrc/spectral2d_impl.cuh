@@ -624,19 +624,6 @@ __device__ __forceinline__ cx<T> jac_x(const cx<T>* __restrict__ A, const cx<T>*
   return d + Cc[(size_t)x * ld + m];
 }
 
-// Linear term op(src) for the point (n, m): 0 value, 1 d/dx, 2 d/dz.
-__device__ __forceinline__ zd lin_term(const GridC& g, zd s, int op, int n, int m) {
-  if (op == 1) {
-    const double b = g.dfx * (double)n;
-    return mk(-(b * s.y), b * s.x);
-  }
-  if (op == 2) {
-    const double b = g.dfz * (double)m;
-    return mk(-(b * s.y), b * s.x);
-  }
-  return s;
-}
-
 // Weighted Adams-Bashforth sum 3 f0 - f1 (AB2) or
 // 55 f0 - 59 f1 + 37 f2 - 9 f3 (AB4) (melvin/Integrator.py:5-18) of the
 // newest value f0 and the previous ones hp[i] = f_{-1-i}; the dt/2 or dt/24
@@ -764,9 +751,15 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, F * sbuf_elems<T, C>(N) * sizeo
 #pragma unroll
           for (int q2 = 1; q2 < F; ++q2)
             if (sidx == q2) sv = qo[u][q2];
-          const zd v = lin_term(g, sv, eq.top[t], n, m);
-          const double cc = tco ? tco[f * 4 + t] : eq.tcoef[t];
-          fv = mk(fv.x + cc * v.x, fv.y + cc * v.y);
+          // d/dx, d/dz: the factor 2 pi n / lx or 2 pi m / lz rides on the
+          // coefficient and i on the value (one product fewer per term)
+          double cc = tco ? tco[f * 4 + t] : eq.tcoef[t];
+          const int op = eq.top[t];
+          if (op != 0) {
+            cc *= op == 1 ? g.dfx * (double)n : g.dfz * (double)m;
+            sv = mk(-sv.y, sv.x);
+          }
+          fv = mk(fv.x + cc * sv.x, fv.y + cc * sv.y);
         }
         const zd cff = cf[u][f], q0 = qo[u][f];
         zd qn;
