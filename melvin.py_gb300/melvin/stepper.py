@@ -161,14 +161,15 @@ class Stepper:
 
         ``states[i]`` and ``histories[i]`` are pinned CPU tensors shaped like
         field i's state and history (the device tensors are the staging
-        copies).  On the current stream the states go up, the step runs, and
-        the states and the history slot the step writes come back.  The
-        history slots the update reads go up on a second stream, and the
-        update (kernel 2, mgb_step_waits) waits for them, so that upload
-        overlaps the transforms; the slot the step overwrites whole is not
-        uploaded.  Fully spectral plans.  Returns the bytes copied up and
-        down; the host tensors hold the result once the current stream has
-        passed this point."""
+        copies).  On the current stream the states go up, the step runs and
+        the states come back.  On a second stream the history slots the
+        update reads go up, overlapping the transforms (the update, kernel 2,
+        waits for them through mgb_step_waits), and after the states the slot
+        the step wrote comes back, overlapping what the current stream runs
+        next.  The slot the step overwrites whole is not uploaded.  Fully
+        spectral plans.  Returns the bytes copied up and down.  The host
+        tensors hold the result once the event ``host_done`` has completed; a
+        later call orders its copies after it."""
         if self.plan.grid.fdm_z:
             raise NotImplementedError("step_host: fully spectral plans only")
         dt = self.sim._integrator._dt if dt is None else dt
@@ -177,12 +178,14 @@ class Stepper:
         if getattr(self, "_copy_stream", None) is None:
             self._copy_stream = torch.cuda.Stream(device=self.device)
             self._hist_ready = torch.cuda.Event()
+            self._states_down = torch.cuda.Event()
+            self.host_done = torch.cuda.Event(enable_timing=True)
         cs = self._copy_stream
         curr = self.fields[0].dvar._curr_idx
         order = self.fields[0].dvar._data.shape[0]
         read = [s for s in range(order) if s != curr]
         up = down = 0
-        cs.wait_stream(main)  # the previous download into these host tensors has finished
+        cs.wait_stream(main)  # after the current stream's earlier work (the step before read these slots)
         with torch.cuda.stream(cs):
             for f, h in zip(self.fields, histories):
                 for s in read:
@@ -200,9 +203,19 @@ class Stepper:
         N.check(self.plan.lib.mgb_step_waits(
             self.plan.handle, C.byref(self.eq), self._q, self._h, curr, float(dt), N.ptr(self.work), None,
             N.stream_handle(self.device), waits, 3))
-        for f, hs, hh in zip(self.fields, states, histories):
+        for f, hs in zip(self.fields, states):
             hs.copy_(f.var._sdata, non_blocking=True)
-            hh[curr].copy_(f.dvar._data[curr], non_blocking=True)
-            down += hs.numel() * hs.element_size() + hh[curr].numel() * hh.element_size()
+            down += hs.numel() * hs.element_size()
+        # the written history slot goes down on the second stream once the
+        # states are down (two downloads at once share one direction's
+        # bandwidth), so it overlaps whatever the current stream runs next
+        self._states_down.record(main)
+        cs.wait_event(self._states_down)
+        with torch.cuda.stream(cs):
+            for f, hh in zip(self.fields, histories):
+                hh[curr].copy_(f.dvar._data[curr], non_blocking=True)
+                down += hh[curr].numel() * hh.element_size()
+            self.host_done.record(cs)
+        for f in self.fields:
             f.dvar.advance()
         return up, down
