@@ -693,7 +693,8 @@ __global__ void __launch_bounds__(NT, (Occ<T, N, F * sbuf_elems<T, C>(N) * sizeo
 #pragma unroll
   for (int f = 0; f < F; ++f) block_fft<T, N, C, C, NT, -1, RM>(buf + f * sbuf_elems<T, C>(N), (const cx<T>*)a.tw);
 
-  // -1/(nx*nz) is a power of two for the grids built, so scaling in T is exact
+  // the transform already holds -J / (nx*nz): the z pass's output scales and
+  // this pass's stencil factor carry the normalisation (powers of two)
   const size_t slot = (size_t)g.rows * g.cols;
   zd* qf[F];
   zd* hf[F];
